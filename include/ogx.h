@@ -1,0 +1,137 @@
+/*
+ * ogx.h -- C ABI of the GB300 batched GJK distance / EPA penetration engine.
+ *
+ * Every function returns an ogx_status (0 = OGX_OK); on failure
+ * ogx_last_error() gives a message for the calling thread.  There is no CPU
+ * fallback: without a usable GPU the calls fail with OGX_ERR_NO_DEVICE.
+ *
+ * Two layers:
+ *   1. Engine API (ogx_ctx / ogx_pool): a device-resident polytope pool in the
+ *      engine's padded SoA layout, batched queries over pairs of pool indices on
+ *      device buffers, asynchronous on the context's stream.
+ *   2. Reference-compatible entry points (ogx_compute_*, ogx_allocate_*, ...):
+ *      the functions of OpenGJK-GPU's host API with the same arguments, meaning
+ *      and output conventions, each replacing the reference function cited beside
+ *      it.  opengjk_gpu.hpp wraps them under the reference's C++ names
+ *      (GJK::GPU::computeDistances, compute_minimum_distance, ...).
+ *
+ * Output conventions (as the reference, GJK/gpu/openGJK.h:52-64, GJK/cpu/EPA.c):
+ *   distance >= 0 for separated pairs, 0 when GJK finds the origin enclosed, and
+ *   -penetration depth after EPA; witnesses in simplex.witnesses[0] (body 1) and
+ *   [1] (body 2); contact normal unit length from body 1 towards body 2, (1,0,0)
+ *   when undefined.
+ */
+#ifndef OGX_H_
+#define OGX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "ogx_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ogx_status;
+#define OGX_OK 0
+#define OGX_ERR_INVALID (-1)   /* bad argument: null pointer, negative size, bad index */
+#define OGX_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define OGX_ERR_NOMEM (-3)     /* device or pinned host allocation failed */
+#define OGX_ERR_NO_DEVICE (-4) /* no usable GPU */
+#define OGX_ERR_CAPACITY (-5)  /* a size exceeds a capacity of the call */
+
+/* Run-time tolerances.  ogx_config_default() fills the engine defaults (FP32 bulk,
+ * FP64 escalation and polish, distances to ~1e-5 relative of the FP64 oracle);
+ * ogx_config_reference() the reference's FP32 constants (GJK/cpu/openGJK.c:41-42,
+ * 955; GJK/cpu/EPA.c:46, 592). */
+typedef struct ogx_config {
+  float gjk_eps_rel;  /* GJK stops when |v|^2 - v.w <= eps_rel |v|^2 */
+  float gjk_eps_tot;  /* ... or when |v|^2 - v.w < eps_tot */
+  float gjk_noise;    /* ... or when |v|^2 - v.w is below noise * FLT_EPSILON |v|(|v|+|w|) */
+  int gjk_max_iter;   /* GJK iteration cap (reference: 25) */
+  float epa_tol;      /* EPA stops when the support improves the closest face by < tol */
+  float epa_rel;      /* ... or by < epa_rel * (scale of the polytope) */
+  float epa_vis;      /* face visibility threshold relative to the polytope scale */
+  int epa_max_iter;   /* EPA iteration cap (reference: 64) */
+  int flags;          /* OGX_FLAG_* */
+  float polish_rel;   /* FP64 re-solve when the FP32 distance bound exceeds this */
+} ogx_config;
+
+#define OGX_FLAG_FP64_ESCALATE 1 /* near-degenerate steps re-run in FP64 */
+#define OGX_FLAG_FP64_POLISH 2   /* final simplex / EPA face re-solved in FP64 */
+#define OGX_FLAG_REFERENCE_TOL 4 /* reference termination rules */
+
+/* Per-pair status bits (optional output of the engine API). */
+#define OGX_PAIR_GJK_CAP 1
+#define OGX_PAIR_GJK_ESCALATED 2
+#define OGX_PAIR_POLISHED 4
+#define OGX_PAIR_EPA_RUN 8
+#define OGX_PAIR_EPA_CONVERGED 16
+#define OGX_PAIR_EPA_DUPLICATE 32
+#define OGX_PAIR_EPA_CAP 64
+#define OGX_PAIR_EPA_TOUCH 128
+#define OGX_PAIR_EPA_TOPOLOGY 256
+#define OGX_PAIR_EPA_CAPACITY 512
+#define OGX_PAIR_EPA_ESCALATED 1024
+#define OGX_PAIR_BAD_INPUT 16384
+
+ogx_status ogx_config_default(ogx_config* cfg);
+ogx_status ogx_config_reference(ogx_config* cfg);
+const char* ogx_status_string(ogx_status s);
+const char* ogx_last_error(void);
+/* library version string and the CUDA architecture it was built for */
+const char* ogx_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* Engine API                                                                 */
+
+typedef struct ogx_ctx ogx_ctx;
+typedef struct ogx_pool ogx_pool;
+
+/* Context on `device` (current device when < 0).  `stream` is a cudaStream_t (NULL:
+ * the context creates its own non-blocking stream).  cfg NULL = defaults. */
+ogx_status ogx_ctx_create(int device, const ogx_config* cfg, void* stream, ogx_ctx** out);
+ogx_status ogx_ctx_destroy(ogx_ctx* ctx);
+ogx_status ogx_ctx_set_config(ogx_ctx* ctx, const ogx_config* cfg);
+ogx_status ogx_ctx_get_config(const ogx_ctx* ctx, ogx_config* cfg);
+ogx_status ogx_ctx_set_stream(ogx_ctx* ctx, void* stream);
+void* ogx_ctx_stream(const ogx_ctx* ctx);
+ogx_status ogx_ctx_synchronize(ogx_ctx* ctx);
+
+/* Pool of num_bodies polytopes; body b has counts[b] >= 1 points (host array).
+ * Device memory: 12 bytes per point plus padding to 4 points per body. */
+ogx_status ogx_pool_create(ogx_ctx* ctx, int num_bodies, const int32_t* counts, ogx_pool** out);
+ogx_status ogx_pool_destroy(ogx_pool* pool);
+int ogx_pool_num_bodies(const ogx_pool* pool);
+int64_t ogx_pool_num_points(const ogx_pool* pool);
+/* Load all points: xyz interleaved, bodies concatenated in index order (host memory,
+ * pinned or pageable).  Asynchronous on the context's stream; pageable sources are
+ * staged through the context's pinned buffer. */
+ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* pool, const float* coords);
+/* Same from device memory (xyz interleaved, concatenated): a packing kernel. */
+ogx_status ogx_pool_load_device(ogx_ctx* ctx, ogx_pool* pool, const float* d_coords);
+/* Device pointer of the SoA points and of the per-body {quad offset, count} table
+ * (for callers that write the pool with their own kernels). */
+ogx_status ogx_pool_device_layout(const ogx_pool* pool, float** d_points, void** d_bodies);
+
+/* GJK over npairs pairs of pool indices (device buffers, asynchronous).
+ * d_status may be NULL. */
+ogx_status ogx_gjk(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkCollisionPair* d_pairs,
+                   gkSimplex* d_simplices, float* d_distances, int32_t* d_status);
+/* GJK then EPA on the pairs in contact (fused pipeline; d_normals n*3 floats). */
+ogx_status ogx_gjk_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                       const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                       float* d_distances, float* d_normals, int32_t* d_status);
+/* EPA only, from simplices and distances of an earlier GJK (in/out). */
+ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkCollisionPair* d_pairs,
+                   gkSimplex* d_simplices, float* d_distances, float* d_normals,
+                   int32_t* d_status);
+
+/* Kernels launched by the last engine call on this context (for accounting). */
+int ogx_ctx_last_launches(const ogx_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OGX_H_ */

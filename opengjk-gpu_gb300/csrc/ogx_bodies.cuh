@@ -1,0 +1,115 @@
+// ogx_bodies.cuh -- where the two bodies of a pair are read from during the scans.
+//
+// Two sources implement the same interface:
+//   MemBodies   -- every scan re-reads the body from memory (host test build, and the
+//                  device path for bodies too large to keep in registers)
+//   RegBodies   -- device only: each lane of the team keeps K float4 blocks of x, y and
+//                  z of both bodies in registers for the whole GJK/EPA run, so the pool
+//                  is read from HBM exactly once per pair.
+// scan() returns the lane-local best (value, index) of <point, d>; the caller combines
+// lanes with team.argmax (max value, ties to the smaller index).
+#pragma once
+
+#include "ogx_common.cuh"
+
+namespace ogx {
+
+struct MemBodies {
+  const float* base[2];  // x[0] of each body
+  int n[2];
+  int n4[2];
+
+  OGX_HD void bind(const float* pool, BodyRef a, BodyRef b) {
+    base[0] = pool + 4 * (size_t)a.quad;
+    base[1] = pool + 4 * (size_t)b.quad;
+    n[0] = a.n;
+    n[1] = b.n;
+    n4[0] = round4(a.n);
+    n4[1] = round4(b.n);
+  }
+  OGX_HD fv3 point(int w, int i) const {
+    const float* p = base[w];
+    return v3<float>(p[i], p[n4[w] + i], p[2 * n4[w] + i]);
+  }
+  OGX_HD dv3 dpoint(int w, int i) const { return cvt<double>(point(w, i)); }
+
+  template <class Team>
+  OGX_HD void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {
+    best = -INFINITY;
+    bi = 0x7fffffff;
+    const int nb = n4[w] >> 2;
+    const float* X = base[w];
+    const float* Y = X + n4[w];
+    const float* Z = X + 2 * n4[w];
+    for (int q = t.lane(); q < nb; q += Team::L) {
+#if defined(__CUDA_ARCH__)
+      const float4 x = __ldg(reinterpret_cast<const float4*>(X) + q);
+      const float4 y = __ldg(reinterpret_cast<const float4*>(Y) + q);
+      const float4 z = __ldg(reinterpret_cast<const float4*>(Z) + q);
+      const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w},
+                  zs[4] = {z.x, z.y, z.z, z.w};
+#else
+      const float* xs = X + 4 * q;
+      const float* ys = Y + 4 * q;
+      const float* zs = Z + 4 * q;
+#endif
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float v = sdot(xs[c], ys[c], zs[c], d);
+        if (v > best) {
+          best = v;
+          bi = 4 * q + c;
+        }
+      }
+    }
+  }
+};
+
+#if defined(__CUDACC__)
+template <int L, int K>
+struct RegBodies {
+  float4 x[2][K], y[2][K], z[2][K];
+  MemBodies mem;  // for point() lookups by index
+
+  __device__ void bind(const float* pool, BodyRef a, BodyRef b, int lane) {
+    mem.bind(pool, a, b);
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+      const int nb = mem.n4[w] >> 2;
+      const float4* X = reinterpret_cast<const float4*>(mem.base[w]);
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        const int q = lane + j * L;
+        const int qq = q < nb ? q : 0;  // beyond the body: repeat block 0 (never wins)
+        x[w][j] = __ldg(X + qq);
+        y[w][j] = __ldg(X + nb + qq);
+        z[w][j] = __ldg(X + 2 * nb + qq);
+      }
+    }
+  }
+  __device__ fv3 point(int w, int i) const { return mem.point(w, i); }
+  __device__ dv3 dpoint(int w, int i) const { return mem.dpoint(w, i); }
+
+  template <class Team>
+  __device__ void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {
+    best = -INFINITY;
+    bi = 0x7fffffff;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const int q4 = 4 * (t.lane() + j * L);
+      const float4 X = x[w][j], Y = y[w][j], Z = z[w][j];
+      float v;
+      v = sdot(X.x, Y.x, Z.x, d);
+      if (v > best) { best = v; bi = q4; }
+      v = sdot(X.y, Y.y, Z.y, d);
+      if (v > best) { best = v; bi = q4 + 1; }
+      v = sdot(X.z, Y.z, Z.z, d);
+      if (v > best) { best = v; bi = q4 + 2; }
+      v = sdot(X.w, Y.w, Z.w, d);
+      if (v > best) { best = v; bi = q4 + 3; }
+    }
+  }
+};
+#endif
+
+}  // namespace ogx

@@ -1,0 +1,280 @@
+// ogx_common.cuh -- shared definitions of the batched GJK/EPA engine.
+//
+// Everything in the per-pair algorithm is written once as __host__ __device__ code over
+// a "team" of L lanes (SPMD: every lane of the team runs the same code and holds the
+// same per-pair state; lanes only split the vertex scans and the EPA face loops).
+// On the GPU a team is L lanes of one warp (L = 4, 8, 16 or 32).  The host build
+// (SerialTeam, L = 1) exists so that the algorithm can be checked on a CPU-only
+// machine; it is compiled into a separate test library, never into the product.
+//
+// Arithmetic is compiled without contraction on both sides (nvcc --fmad=false,
+// g++ -ffp-contract=off); where a fused multiply-add is wanted it is written as
+// fmaf() explicitly, so the host build and the device build round identically.
+#pragma once
+
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "ogx.h"
+
+#if defined(__CUDACC__)
+#define OGX_HD __host__ __device__ __forceinline__
+#define OGX_D __device__ __forceinline__
+#else
+#define OGX_HD inline
+#endif
+
+#if !defined(__CUDACC__)
+// the two CUDA vector types the algorithm uses, for the host build
+struct float4 {
+  float x, y, z, w;
+};
+struct int2 {
+  int x, y;
+};
+#endif
+
+namespace ogx {
+
+OGX_HD float4 make_float4_(float x, float y, float z, float w) {
+  float4 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  r.w = w;
+  return r;
+}
+OGX_HD int2 make_int2_(int x, int y) {
+  int2 r;
+  r.x = x;
+  r.y = y;
+  return r;
+}
+
+// ----------------------------------------------------------------------------------
+// small vectors
+
+struct f3 {
+  float x, y, z;
+};
+struct d3 {
+  double x, y, z;
+};
+
+template <class T>
+struct vec3 {
+  T x, y, z;
+};
+
+template <class T>
+OGX_HD vec3<T> v3(T x, T y, T z) {
+  vec3<T> r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+template <class T>
+OGX_HD vec3<T> operator-(vec3<T> a, vec3<T> b) {
+  return v3<T>(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+template <class T>
+OGX_HD vec3<T> operator+(vec3<T> a, vec3<T> b) {
+  return v3<T>(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+template <class T>
+OGX_HD vec3<T> operator-(vec3<T> a) {
+  return v3<T>(-a.x, -a.y, -a.z);
+}
+template <class T>
+OGX_HD vec3<T> operator*(vec3<T> a, T s) {
+  return v3<T>(a.x * s, a.y * s, a.z * s);
+}
+template <class T>
+OGX_HD T dot(vec3<T> a, vec3<T> b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <class T>
+OGX_HD vec3<T> cross(vec3<T> a, vec3<T> b) {
+  return v3<T>(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <class T>
+OGX_HD T l1(vec3<T> a) {
+  return fabs(a.x) + fabs(a.y) + fabs(a.z);
+}
+OGX_HD float l1(vec3<float> a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
+
+template <class T, class U>
+OGX_HD vec3<T> cvt(vec3<U> a) {
+  return v3<T>((T)a.x, (T)a.y, (T)a.z);
+}
+
+typedef vec3<float> fv3;
+typedef vec3<double> dv3;
+
+// Support-scan dot product.  Written with explicit fused multiply-adds so that the
+// value of a vertex is the same wherever it is evaluated (scan, previous support).
+OGX_HD float sdot(float x, float y, float z, fv3 d) { return fmaf(z, d.z, fmaf(y, d.y, x * d.x)); }
+OGX_HD float sdot(fv3 p, fv3 d) { return sdot(p.x, p.y, p.z, d); }
+
+// ----------------------------------------------------------------------------------
+// run-time configuration and per-pair status
+
+// Tolerances of one engine instance: the public ogx_config (include/ogx.h).
+typedef ::ogx_config Config;
+
+enum {
+  OGX_F_FP64_ESCALATE = OGX_FLAG_FP64_ESCALATE,  // near-degenerate steps re-run in FP64
+  OGX_F_FP64_POLISH = OGX_FLAG_FP64_POLISH,      // final simplex / face re-solved in FP64
+  OGX_F_REFERENCE_TOL = OGX_FLAG_REFERENCE_TOL,  // reference termination rules
+};
+
+// Per-pair status bits written beside the results.
+enum {
+  OGX_S_GJK_CAP = OGX_PAIR_GJK_CAP,
+  OGX_S_GJK_ESCALATED = OGX_PAIR_GJK_ESCALATED,
+  OGX_S_POLISHED = OGX_PAIR_POLISHED,
+  OGX_S_EPA_RUN = OGX_PAIR_EPA_RUN,
+  OGX_S_EPA_CONVERGED = OGX_PAIR_EPA_CONVERGED,
+  OGX_S_EPA_DUPLICATE = OGX_PAIR_EPA_DUPLICATE,
+  OGX_S_EPA_CAP = OGX_PAIR_EPA_CAP,
+  OGX_S_EPA_TOUCH = OGX_PAIR_EPA_TOUCH,
+  OGX_S_EPA_TOPOLOGY = OGX_PAIR_EPA_TOPOLOGY,
+  OGX_S_EPA_CAPACITY = OGX_PAIR_EPA_CAPACITY,
+  OGX_S_EPA_ESCALATED = OGX_PAIR_EPA_ESCALATED,
+  OGX_S_BAD_INPUT = OGX_PAIR_BAD_INPUT,
+};
+
+OGX_HD Config default_config() {
+  Config c;
+  c.gjk_eps_rel = 1e-6f;
+  c.gjk_eps_tot = 1e-24f;
+  c.gjk_noise = 8.0f;
+  c.gjk_max_iter = 32;
+  c.epa_tol = 1e-6f;
+  c.epa_rel = 2e-6f;
+  c.epa_vis = 1e-6f;
+  c.epa_max_iter = 64;
+  c.flags = OGX_F_FP64_ESCALATE | OGX_F_FP64_POLISH;
+  c.polish_rel = 2e-6f;
+  return c;
+}
+
+// The reference's FP32 constants (GJK/cpu/openGJK.c:41-42,955; GJK/cpu/EPA.c:46,592).
+OGX_HD Config reference_config() {
+  Config c = default_config();
+  c.gjk_eps_rel = FLT_EPSILON * 1e4f;
+  c.gjk_eps_tot = FLT_EPSILON * 1e2f;
+  c.gjk_noise = 0.0f;
+  c.gjk_max_iter = 25;
+  c.epa_tol = FLT_EPSILON * 1e2f;
+  c.epa_rel = 0.0f;
+  c.epa_vis = 0.0f;
+  c.epa_max_iter = 64;
+  c.flags = OGX_F_REFERENCE_TOL;
+  c.polish_rel = 0.0f;
+  return c;
+}
+
+// EPA capacities.  With at most 64 expansions the polytope has at most 68 vertices and
+// (Euler, closed triangulated surface) 2*68-4 = 132 faces.
+constexpr int kEpaVmax = 68;
+constexpr int kEpaFmax = 132;
+
+// ----------------------------------------------------------------------------------
+// teams
+
+// Host team of one lane (test build).
+struct SerialTeam {
+  static constexpr int L = 1;
+  OGX_HD int lane() const { return 0; }
+  OGX_HD void argmax(float&, int&) const {}
+  OGX_HD void argmin(float&, int&) const {}
+  OGX_HD bool any(bool p) const { return p; }
+  OGX_HD int excl_scan(int x, int& total) const {
+    total = x;
+    return 0;
+  }
+  OGX_HD int imax(int x) const { return x; }
+  OGX_HD float fmax_(float x) const { return x; }
+  OGX_HD void sync() const {}
+};
+
+#if defined(__CUDACC__)
+// L consecutive lanes of a warp (L a power of two <= 32).
+template <int L_>
+struct WarpTeam {
+  static constexpr int L = L_;
+  unsigned mask;
+  int ln;
+  __device__ WarpTeam() {
+    const int wl = threadIdx.x & 31;
+    ln = wl & (L - 1);
+    mask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (wl & ~(L - 1)));
+  }
+  __device__ int lane() const { return ln; }
+  // max value, ties to the smaller index
+  __device__ void argmax(float& v, int& i) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      const float v2 = __shfl_xor_sync(mask, v, o);
+      const int i2 = __shfl_xor_sync(mask, i, o);
+      if (v2 > v || (v2 == v && i2 < i)) {
+        v = v2;
+        i = i2;
+      }
+    }
+  }
+  // min value, ties to the smaller index (index -1 means "none" and loses)
+  __device__ void argmin(float& v, int& i) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      const float v2 = __shfl_xor_sync(mask, v, o);
+      const int i2 = __shfl_xor_sync(mask, i, o);
+      const bool take = (i < 0) ? (i2 >= 0) : (i2 >= 0 && (v2 < v || (v2 == v && i2 < i)));
+      if (take) {
+        v = v2;
+        i = i2;
+      }
+    }
+  }
+  __device__ bool any(bool p) const { return (__ballot_sync(mask, p) & mask) != 0u; }
+  __device__ int excl_scan(int x, int& total) const {
+    int inc = x;
+#pragma unroll
+    for (int o = 1; o < L; o <<= 1) {
+      const int y = __shfl_up_sync(mask, inc, o, L);
+      if (ln >= o) inc += y;
+    }
+    total = __shfl_sync(mask, inc, L - 1, L);
+    return inc - x;
+  }
+  __device__ int imax(int x) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) x = max(x, __shfl_xor_sync(mask, x, o));
+    return x;
+  }
+  __device__ float fmax_(float x) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) x = fmaxf(x, __shfl_xor_sync(mask, x, o));
+    return x;
+  }
+  __device__ void sync() const { __syncwarp(mask); }
+};
+#endif
+
+// ----------------------------------------------------------------------------------
+// pool layout
+//
+// Body b occupies 3 * n4 floats starting at float offset 4 * quad[b] of the pool:
+// x[0..n4), y[0..n4), z[0..n4), n4 = n rounded up to a multiple of 4.  The padding
+// points repeat point 0, so they never win a support scan (ties go to the lower index).
+struct BodyRef {
+  uint32_t quad;  // offset of x[0] in float4 units
+  int32_t n;      // number of points
+};
+
+OGX_HD int round4(int n) { return (n + 3) & ~3; }
+
+}  // namespace ogx

@@ -1,0 +1,542 @@
+// ogx_epa.cuh -- EPA penetration depth for one colliding pair, run by a team of L lanes.
+//
+// Semantics follow the reference's computeCollisionInformation (GJK/cpu/EPA.c:362-863,
+// GJK/gpu/openGJK.cu:1836-2726): a separated pair only gets its contact normal
+// (normalised w1 - w0); a contact whose GJK simplex has fewer than four points is grown
+// by supports along fixed directions (point, edge-perpendicular, triangle normal and its
+// opposite) and reported with depth 0 when no new point appears; otherwise the simplex
+// seeds a polytope that is expanded towards its closest face until the support point
+// along that face's normal does not improve on it.  The result is depth = -distance of
+// the closest face, its normal, and witnesses from the origin's barycentric position on
+// that face (clamped to the triangle as in EPA.c:238-304).
+//
+// Design (not the reference's):
+//  * The polytope keeps face adjacency.  The faces visible from the new point are found
+//    in parallel (faces are split over the lanes), the horizon is every edge of a visible
+//    face whose neighbour is not visible, and new faces are linked to each other through
+//    two per-vertex tables -- O(F) per step instead of the reference's O(F^2) edge
+//    de-duplication.  Winding is inherited from the horizon edge, so no centroid test.
+//  * Face normals are computed once when the face is created (the reference recomputes
+//    all of them every step) in FP32, in FP64 from the exact points for sliver faces.
+//  * Polytope capacity is 68 vertices / 132 faces, enough for the 64-step cap (the
+//    reference's 128-face list can overflow in its last steps).
+//  * Duplicate detection compares the support pair's vertex indices.
+//  * The chosen face can be re-solved in FP64 afterwards (same pass as the GJK polish).
+#pragma once
+
+#include "ogx_common.cuh"
+#include "ogx_gjk.cuh"
+
+namespace ogx {
+
+// Shared-memory working set of one pair (5728 bytes).
+struct EpaMem {
+  float4 fn[kEpaFmax];          // unit outward normal, w = plane distance from origin
+  float4 vp[kEpaVmax];          // polytope vertices (Minkowski points)
+  int2 vid[kEpaVmax];           // (index in body 1, index in body 2)
+  uint8_t fv[kEpaFmax][4];      // face vertices a, b, c; [3] = 1 when the face is alive
+  uint8_t fa[kEpaFmax][4];      // fa[f][e]: face across edge e = (v_e, v_{e+1 mod 3})
+  uint8_t vis[kEpaFmax];        // visible from the new point (this step)
+  uint8_t freel[kEpaFmax];      // free face slots (this step)
+  uint8_t hz[kEpaFmax][4];      // horizon edges (this step): a, b, face beyond
+  uint8_t hstart[kEpaVmax];     // new face whose horizon edge starts at vertex
+  uint8_t hend[kEpaVmax];       // new face whose horizon edge ends at vertex
+};
+
+struct EpaOut {
+  float dist;   // -depth for contacts, the GJK distance otherwise
+  fv3 w0, w1;   // witnesses
+  fv3 nrm;      // contact normal, body 1 -> body 2
+  int status;
+  int iters;
+  int face[3][2];  // vertex index pairs of the final face (FP64 re-solve)
+  bool polish;
+};
+
+OGX_HD fv3 unit_or_x(fv3 d) {
+  const float n = sqrtf(dot(d, d));
+  if (n > FLT_EPSILON) return d * (1.0f / n) ;
+  return v3<float>(1.0f, 0.0f, 0.0f);
+}
+
+// support of the Minkowski difference along d (first maximum wins, EPA.c:307-344)
+template <class Team, class Bodies>
+OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
+  float ba, bb;
+  B.scan(t, 0, d, ba, ia);
+  B.scan(t, 1, -d, bb, ib);
+  t.argmax(ba, ia);
+  t.argmax(bb, ib);
+  return B.point(0, ia) - B.point(1, ib);
+}
+
+// plane of face (a, b, c): FP32, FP64 from exact points for slivers
+template <class Bodies>
+OGX_HD float4 face_plane(const EpaMem& M, const Bodies& B, int a, int b, int c, bool escalate,
+                         int& status) {
+  const float4 P0 = M.vp[a], P1 = M.vp[b], P2 = M.vp[c];
+  const fv3 p0 = v3<float>(P0.x, P0.y, P0.z);
+  const fv3 e0 = v3<float>(P1.x, P1.y, P1.z) - p0;
+  const fv3 e1 = v3<float>(P2.x, P2.y, P2.z) - p0;
+  const fv3 n = cross(e0, e1);
+  const float nn = dot(n, n);
+  const float s = l1(e0) * l1(e1);
+  float4 r;
+  if (escalate && nn < 1e-6f * s * s) {
+    // sine of the face angle below ~1e-3: FP32 normal unreliable
+    const dv3 q0 = B.dpoint(0, M.vid[a].x) - B.dpoint(1, M.vid[a].y);
+    const dv3 q1 = B.dpoint(0, M.vid[b].x) - B.dpoint(1, M.vid[b].y);
+    const dv3 q2 = B.dpoint(0, M.vid[c].x) - B.dpoint(1, M.vid[c].y);
+    const dv3 m = cross(q1 - q0, q2 - q0);
+    const double mm = dot(m, m);
+    status |= OGX_S_EPA_ESCALATED;
+    if (mm > 0.0) {
+      const double inv = 1.0 / sqrt(mm);
+      r.x = (float)(m.x * inv);
+      r.y = (float)(m.y * inv);
+      r.z = (float)(m.z * inv);
+      r.w = (float)(dot(m, q0) * inv);
+    } else {
+      r.x = r.y = r.z = 0.0f;
+      r.w = INFINITY;  // degenerate: never the closest face, never visible
+    }
+    return r;
+  }
+  if (nn > 0.0f) {
+    const float inv = 1.0f / sqrtf(nn);
+    r.x = n.x * inv;
+    r.y = n.y * inv;
+    r.z = n.z * inv;
+    r.w = r.x * p0.x + r.y * p0.y + r.z * p0.z;
+  } else {
+    r.x = r.y = r.z = 0.0f;
+    r.w = INFINITY;
+  }
+  return r;
+}
+
+// barycentric weights of the origin's projection on triangle (p0, p1, p2), clamped to
+// the triangle's edges as EPA.c:238-304 does
+OGX_HD int tri_weights(fv3 p0, fv3 p1, fv3 p2, float* l) {
+  const fv3 e0 = p1 - p0, e1 = p2 - p0;
+  const float d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1);
+  const float d20 = -dot(p0, e0), d21 = -dot(p0, e1);
+  const float den = d00 * d11 - d01 * d01;
+  if (fabsf(den) < FLT_EPSILON) {
+    l[0] = l[1] = l[2] = 1.0f / 3.0f;
+    return -1;
+  }
+  const float inv = 1.0f / den;
+  const float u = (d11 * d20 - d01 * d21) * inv;
+  const float v = (d00 * d21 - d01 * d20) * inv;
+  const float w = 1.0f - u - v;
+  if (w < 0.0f) {
+    const fv3 e12 = p2 - p1;
+    float tt = -dot(p1, e12) / dot(e12, e12);
+    tt = fmaxf(0.0f, fminf(1.0f, tt));
+    l[0] = 0.0f;
+    l[1] = 1.0f - tt;
+    l[2] = tt;
+    return 1;  // beyond edge p1-p2 (edge 1 of the face)
+  } else if (u < 0.0f) {
+    float tt = -dot(p0, e1) / dot(e1, e1);
+    tt = fmaxf(0.0f, fminf(1.0f, tt));
+    l[0] = 1.0f - tt;
+    l[1] = 0.0f;
+    l[2] = tt;
+    return 2;  // beyond edge p2-p0
+  } else if (v < 0.0f) {
+    float tt = -dot(p0, e0) / dot(e0, e0);
+    tt = fmaxf(0.0f, fminf(1.0f, tt));
+    l[0] = 1.0f - tt;
+    l[1] = tt;
+    l[2] = 0.0f;
+    return 0;  // beyond edge p0-p1
+  }
+  l[0] = w;
+  l[1] = u;
+  l[2] = v;
+  return -1;
+}
+
+// Result from face f.  When the origin's projection falls outside f and the face across
+// that edge lies in the same plane (the Minkowski face of an edge-edge or face-face
+// contact is split into coplanar triangles), the neighbour that holds the projection is
+// used, so that w0 - w1 = depth * normal holds.
+template <class Bodies>
+OGX_HD void epa_emit(const EpaMem& M, const Bodies& B, int f, float tie, EpaOut& o) {
+  int a = M.fv[f][0], b = M.fv[f][1], c = M.fv[f][2];
+  float l[3];
+  for (int hop = 0; hop < 4; ++hop) {
+    a = M.fv[f][0];
+    b = M.fv[f][1];
+    c = M.fv[f][2];
+    const float4 P0 = M.vp[a], P1 = M.vp[b], P2 = M.vp[c];
+    const int out = tri_weights(v3<float>(P0.x, P0.y, P0.z), v3<float>(P1.x, P1.y, P1.z),
+                                v3<float>(P2.x, P2.y, P2.z), l);
+    if (out < 0) break;
+    const int g2 = M.fa[f][out];
+    const float4 nf = M.fn[f], ng = M.fn[g2];
+    const bool coplanar = M.fv[g2][3] && fabsf(ng.w - nf.w) <= tie &&
+                          (nf.x * ng.x + nf.y * ng.y + nf.z * ng.z) > 1.0f - 1e-5f;
+    if (!coplanar) break;
+    f = g2;
+  }
+  const int2 ia = M.vid[a], ib = M.vid[b], ic = M.vid[c];
+  o.w0 = B.point(0, ia.x) * l[0] + B.point(0, ib.x) * l[1] + B.point(0, ic.x) * l[2];
+  o.w1 = B.point(1, ia.y) * l[0] + B.point(1, ib.y) * l[1] + B.point(1, ic.y) * l[2];
+  const float4 n = M.fn[f];
+  o.nrm = v3<float>(n.x, n.y, n.z);
+  o.dist = -n.w;
+  o.face[0][0] = ia.x;
+  o.face[0][1] = ia.y;
+  o.face[1][0] = ib.x;
+  o.face[1][1] = ib.y;
+  o.face[2][0] = ic.x;
+  o.face[2][1] = ic.y;
+}
+
+OGX_HD void epa_touch(fv3 a, fv3 b, EpaOut& o) {
+  o.dist = 0.0f;
+  o.w0 = a;
+  o.w1 = b;
+  o.nrm = unit_or_x(b - a);
+  o.status |= OGX_S_EPA_TOUCH;
+}
+
+// exact FP64 re-solve of the final face (plane, depth, witnesses)
+template <class Bodies>
+OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
+  dv3 A[3], Bq[3], Q[3];
+  for (int k = 0; k < 3; ++k) {
+    A[k] = B.dpoint(0, o.face[k][0]);
+    Bq[k] = B.dpoint(1, o.face[k][1]);
+    Q[k] = A[k] - Bq[k];
+  }
+  const dv3 m = cross(Q[1] - Q[0], Q[2] - Q[0]);
+  const double mm = dot(m, m);
+  if (!(mm > 0.0)) return;
+  const double inv = 1.0 / sqrt(mm);
+  dv3 n = m * inv;
+  double d = dot(n, Q[0]);
+  // keep the orientation chosen during the expansion
+  if (n.x * o.nrm.x + n.y * o.nrm.y + n.z * o.nrm.z < 0.0) {
+    n = -n;
+    d = -d;
+  }
+  // barycentric weights of the projection of the origin, clamped like tri_weights
+  const dv3 e0 = Q[1] - Q[0], e1 = Q[2] - Q[0];
+  const double d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1);
+  const double d20 = -dot(Q[0], e0), d21 = -dot(Q[0], e1);
+  const double den = d00 * d11 - d01 * d01;
+  double l[3] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
+  if (fabs(den) > 0.0) {
+    const double u = (d11 * d20 - d01 * d21) / den;
+    const double v = (d00 * d21 - d01 * d20) / den;
+    const double w = 1.0 - u - v;
+    if (w < 0.0) {
+      const dv3 e12 = Q[2] - Q[1];
+      double tt = -dot(Q[1], e12) / dot(e12, e12);
+      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
+      l[0] = 0.0; l[1] = 1.0 - tt; l[2] = tt;
+    } else if (u < 0.0) {
+      double tt = -dot(Q[0], e1) / dot(e1, e1);
+      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
+      l[0] = 1.0 - tt; l[1] = 0.0; l[2] = tt;
+    } else if (v < 0.0) {
+      double tt = -dot(Q[0], e0) / dot(e0, e0);
+      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
+      l[0] = 1.0 - tt; l[1] = tt; l[2] = 0.0;
+    } else {
+      l[0] = w; l[1] = u; l[2] = v;
+    }
+  }
+  const dv3 w0 = A[0] * l[0] + A[1] * l[1] + A[2] * l[2];
+  const dv3 w1 = Bq[0] * l[0] + Bq[1] * l[1] + Bq[2] * l[2];
+  o.w0 = cvt<float>(w0);
+  o.w1 = cvt<float>(w1);
+  o.nrm = cvt<float>(n);
+  o.dist = (float)(-d);
+  o.status |= OGX_S_POLISHED;
+}
+
+// Run EPA for one pair whose GJK result is g.  `M` is this pair's shared working set.
+template <class Team, class Bodies>
+OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const GjkState& g,
+                     EpaMem& M, EpaOut& o) {
+  const int L = Team::L;
+  const int lane = t.lane();
+  const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
+  o.status = 0;
+  o.iters = 0;
+  o.polish = false;
+  o.dist = g.dist;
+  o.w0 = g.w0;
+  o.w1 = g.w1;
+  o.nrm = unit_or_x(g.w1 - g.w0);
+  if (g.n != 4 && g.dist > FLT_EPSILON) return;  // separated (EPA.c:369-373)
+  o.status |= OGX_S_EPA_RUN;
+
+  // ---- grow the simplex to a tetrahedron (EPA.c:375-583)
+  fv3 P[4];
+  int IA[4], IB[4];
+  int n = g.n;
+  for (int j = 0; j < n; ++j) {
+    P[j] = g.P[j];
+    IA[j] = g.ia[j];
+    IB[j] = g.ib[j];
+  }
+  const float e2 = FLT_EPSILON * FLT_EPSILON;
+  auto is_new = [&](fv3 q, int qa, int qb) {
+    for (int j = 0; j < n; ++j) {
+      const fv3 d = q - P[j];
+      if (dot(d, d) < e2 || (IA[j] == qa && IB[j] == qb)) return false;
+    }
+    return true;
+  };
+  if (n == 1) {
+    int qa, qb;
+    const fv3 q = msupport(t, B, P[0], qa, qb);
+    if (!is_new(q, qa, qb)) {
+      epa_touch(B.point(0, qa), B.point(1, qb), o);
+      return;
+    }
+    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+  }
+  if (n == 2) {
+    const fv3 e = P[1] - P[0];
+    fv3 axis = v3<float>(1.0f, 0.0f, 0.0f);
+    const float el = sqrtf(dot(e, e));
+    if (el > FLT_EPSILON && fabsf(e.x) > 0.9f * el) axis = v3<float>(0.0f, 1.0f, 0.0f);
+    fv3 d = cross(e, axis);
+    if (dot(d, d) < FLT_EPSILON) d = cross(e, v3<float>(0.0f, 0.0f, 1.0f));
+    int qa, qb;
+    const fv3 q = msupport(t, B, d, qa, qb);
+    if (!is_new(q, qa, qb)) {
+      epa_touch(B.point(0, qa), B.point(1, qb), o);
+      return;
+    }
+    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+  }
+  if (n == 3) {
+    fv3 d = cross(P[1] - P[0], P[2] - P[0]);
+    int qa, qb;
+    fv3 q = msupport(t, B, d, qa, qb);
+    if (!is_new(q, qa, qb)) {
+      q = msupport(t, B, -d, qa, qb);
+      if (!is_new(q, qa, qb)) {
+        epa_touch(B.point(0, qa), B.point(1, qb), o);
+        return;
+      }
+    }
+    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+  }
+
+  // ---- tetrahedron
+  const float vol = dot(P[1] - P[0], cross(P[2] - P[0], P[3] - P[0]));
+  // outward faces of a positively oriented tetrahedron (0,1,2,3); swap 1 and 2 otherwise
+  const int i1 = vol >= 0.0f ? 1 : 2, i2 = vol >= 0.0f ? 2 : 1;
+  const int tri[4][3] = {{0, i2, i1}, {0, i1, 3}, {i1, i2, 3}, {i2, 0, 3}};
+  float scale2 = 0.0f;
+  for (int j = lane; j < 4; j += L) {
+    M.vp[j] = make_float4_(P[j].x, P[j].y, P[j].z, 0.0f);
+    M.vid[j] = make_int2_(IA[j], IB[j]);
+  }
+  for (int j = 0; j < 4; ++j) scale2 = fmaxf(scale2, dot(P[j], P[j]));
+  for (int f = lane; f < kEpaFmax; f += L) M.fv[f][3] = 0;
+  t.sync();
+  for (int f = lane; f < 4; f += L) {
+    for (int k = 0; k < 3; ++k) M.fv[f][k] = (uint8_t)tri[f][k];
+    M.fv[f][3] = 1;
+    for (int k = 0; k < 3; ++k) {
+      const int a = tri[f][k], b = tri[f][(k + 1) % 3];
+      for (int h = 0; h < 4; ++h)
+        for (int m = 0; m < 3; ++m)
+          if (tri[h][m] == b && tri[h][(m + 1) % 3] == a) M.fa[f][k] = (uint8_t)h;
+    }
+  }
+  t.sync();
+  int st = 0;
+  for (int f = lane; f < 4; f += L) M.fn[f] = face_plane(M, B, M.fv[f][0], M.fv[f][1], M.fv[f][2], escalate, st);
+  int nv = 4, fend = 4;
+  t.sync();
+
+  const float tol_floor = cfg.epa_tol;
+  int it = 0;
+  int best = -1;
+  bool done = false;
+  while (it < cfg.epa_max_iter) {
+    ++it;
+    // closest live face
+    float bd = INFINITY;
+    best = -1;
+    for (int f = lane; f < fend; f += L) {
+      if (!M.fv[f][3]) continue;
+      const float d = M.fn[f].w;
+      if (d < bd) {
+        bd = d;
+        best = f;
+      }
+    }
+    t.argmin(bd, best);
+    if (best < 0 || !(bd < INFINITY)) {
+      o.status |= OGX_S_EPA_TOPOLOGY;
+      best = -1;
+      done = true;
+      break;
+    }
+    const float4 nf = M.fn[best];
+    const fv3 n = v3<float>(nf.x, nf.y, nf.z);
+    int qa, qb;
+    const fv3 q = msupport(t, B, n, qa, qb);
+    const float scale = sqrtf(fmaxf(scale2, dot(q, q)));
+    const float tol = fmaxf(tol_floor, cfg.epa_rel * scale);
+    const float gain = dot(n, q) - bd;
+    if (gain < tol) {
+      o.status |= OGX_S_EPA_CONVERGED;
+      done = true;
+      break;
+    }
+    bool dup = false;
+    for (int j = lane; j < nv; j += L) {
+      const int2 id = M.vid[j];
+      dup |= (id.x == qa && id.y == qb);
+    }
+    if (t.any(dup)) {
+      o.status |= OGX_S_EPA_DUPLICATE;
+      done = true;
+      break;
+    }
+    if (nv >= kEpaVmax) {
+      o.status |= OGX_S_EPA_CAPACITY;
+      done = true;
+      break;
+    }
+    const int p = nv;
+    if (lane == 0) {
+      M.vp[p] = make_float4_(q.x, q.y, q.z, 0.0f);
+      M.vid[p] = make_int2_(qa, qb);
+    }
+    ++nv;
+    scale2 = fmaxf(scale2, dot(q, q));
+    const float vis_eps = cfg.epa_vis * scale;
+
+    // faces seen from q
+    for (int f = lane; f < fend; f += L) {
+      bool s = false;
+      if (M.fv[f][3]) {
+        const float4 fp = M.fn[f];
+        s = (fp.x * q.x + fp.y * q.y + fp.z * q.z) - fp.w > vis_eps;
+      }
+      M.vis[f] = s;
+    }
+    t.sync();
+    // the closest face must be seen (gain >= tol > vis threshold); otherwise stop
+    if (!M.vis[best]) {
+      o.status |= OGX_S_EPA_TOPOLOGY;
+      done = true;
+      break;
+    }
+    // horizon edges (edge e of a visible face whose neighbour is not visible) and free
+    // face slots, compacted over the lanes into hz[] and freel[]
+    int hcount = 0;
+    for (int f = lane; f < fend; f += L) {
+      if (!M.vis[f]) continue;
+      for (int e = 0; e < 3; ++e) hcount += M.vis[M.fa[f][e]] ? 0 : 1;
+    }
+    int fcount = 0;
+    for (int f = lane; f < kEpaFmax; f += L)
+      fcount += (f >= fend || !M.fv[f][3] || M.vis[f]) ? 1 : 0;
+    int htot, ftot;
+    const int hbase = t.excl_scan(hcount, htot);
+    const int fbase = t.excl_scan(fcount, ftot);
+    if (htot > ftot || htot < 3) {
+      o.status |= (htot > ftot) ? OGX_S_EPA_CAPACITY : OGX_S_EPA_TOPOLOGY;
+      done = true;
+      break;
+    }
+    {
+      int k = fbase;
+      for (int f = lane; f < kEpaFmax; f += L)
+        if (f >= fend || !M.fv[f][3] || M.vis[f]) M.freel[k++] = (uint8_t)f;
+      k = hbase;
+      for (int f = lane; f < fend; f += L) {
+        if (!M.vis[f]) continue;
+        for (int e = 0; e < 3; ++e) {
+          const int g2 = M.fa[f][e];
+          if (M.vis[g2]) continue;
+          M.hz[k][0] = M.fv[f][e];
+          M.hz[k][1] = M.fv[f][(e + 1) % 3];
+          M.hz[k][2] = (uint8_t)g2;
+          ++k;
+        }
+      }
+    }
+    t.sync();
+    // relink the faces outside the horizon, index the horizon by its vertices, retire
+    // the visible faces
+    for (int k = lane; k < htot; k += L) {
+      const int s = M.freel[k];
+      const int a = M.hz[k][0], b = M.hz[k][1], g2 = M.hz[k][2];
+      for (int m = 0; m < 3; ++m)
+        if (M.fv[g2][m] == b && M.fv[g2][(m + 1) % 3] == a) M.fa[g2][m] = (uint8_t)s;
+      M.hstart[a] = (uint8_t)s;
+      M.hend[b] = (uint8_t)s;
+    }
+    for (int f = lane; f < fend; f += L)
+      if (M.vis[f]) M.fv[f][3] = 0;
+    t.sync();
+    // a vertex that starts (or ends) two horizon edges means the horizon is not one
+    // simple loop; keep the closest face found this step and stop
+    bool bad = false;
+    for (int k = lane; k < htot; k += L) {
+      const int s = M.freel[k];
+      bad |= (M.hstart[M.hz[k][0]] != s) || (M.hend[M.hz[k][1]] != s);
+    }
+    if (t.any(bad)) {
+      o.status |= OGX_S_EPA_TOPOLOGY;
+      done = true;
+      break;
+    }
+    // new face (a, b, p) across each horizon edge a->b
+    int my_new_max = -1;
+    for (int k = lane; k < htot; k += L) {
+      const int s = M.freel[k];
+      const int a = M.hz[k][0], b = M.hz[k][1];
+      M.fv[s][0] = (uint8_t)a;
+      M.fv[s][1] = (uint8_t)b;
+      M.fv[s][2] = (uint8_t)p;
+      M.fa[s][0] = M.hz[k][2];
+      M.fa[s][1] = M.hstart[b];
+      M.fa[s][2] = M.hend[a];
+      M.fn[s] = face_plane(M, B, a, b, p, escalate, st);
+      M.fv[s][3] = 1;
+      my_new_max = my_new_max > s ? my_new_max : s;
+    }
+    const int new_max = t.imax(my_new_max);
+    fend = fend > new_max + 1 ? fend : new_max + 1;
+    t.sync();
+  }
+  o.iters = it;
+  o.status |= st ? OGX_S_EPA_ESCALATED : 0;
+  if (!done) {
+    // iteration cap: closest current face
+    float bd = INFINITY;
+    best = -1;
+    for (int f = lane; f < fend; f += L) {
+      if (!M.fv[f][3]) continue;
+      if (M.fn[f].w < bd) {
+        bd = M.fn[f].w;
+        best = f;
+      }
+    }
+    t.argmin(bd, best);
+    o.status |= OGX_S_EPA_CAP;
+  }
+  if (best >= 0) {
+    epa_emit(M, B, best, fmaxf(cfg.epa_tol, cfg.epa_rel * sqrtf(scale2)), o);
+    o.polish = (cfg.flags & OGX_F_FP64_POLISH) != 0;
+  }
+}
+
+}  // namespace ogx

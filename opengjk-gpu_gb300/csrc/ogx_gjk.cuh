@@ -1,0 +1,637 @@
+// ogx_gjk.cuh -- GJK distance for one pair, run by a team of L lanes.
+//
+// Algorithm (the reference's GJK, GJK/cpu/openGJK.c:952-1056 and
+// GJK/gpu/openGJK.cu:1253-1425): start from v = A[0] - B[0]; each iteration takes the
+// support points s_A(-v), s_B(v), stops when the new point cannot reduce |v| (relative
+// gap test), otherwise appends w = s_A - s_B to the simplex and runs the signed-volume
+// sub-distance algorithm (Montanari's hff tests, openGJK.c:219-613), which returns the
+// point of the simplex closest to the origin and drops the vertices it does not need.
+//
+// What differs from the reference, and why:
+//  * The support scans are split over the team's lanes and combined with a shuffle
+//    argmax; the tie rule (keep the previous support unless strictly beaten, then the
+//    lowest index) is the reference CPU's rule (openGJK.c:615-639).
+//  * Every lane runs the sub-distance redundantly, so nothing is broadcast.
+//  * The sub-distance runs in FP32.  Each sign decision carries a forward error bound;
+//    if any decision of a step falls inside its bound, the whole step is re-run in FP64
+//    on the exact Minkowski points re-read from the pool (OGX_F_FP64_ESCALATE).
+//  * Termination also stops when the support pair is already in the simplex (no
+//    progress is possible) and when the gap is below FP32 rounding of |v| |w|.
+//  * The final simplex can be re-solved in FP64 (exact closest point of the final
+//    feature) when the FP32 distance is not known to polish_rel (OGX_F_FP64_POLISH);
+//    on the device that runs as a separate pass over the pairs that need it.
+#pragma once
+
+#include "ogx_common.cuh"
+
+namespace ogx {
+
+template <class T>
+struct Eps {
+  static constexpr double v = 0.0;
+};
+template <>
+struct Eps<float> {
+  static constexpr double v = FLT_EPSILON;
+};
+
+// flag set when a decision falls inside its rounding bound
+struct Unc {
+  bool hit;
+};
+
+template <class T>
+struct Vx {
+  vec3<T> p;
+  int k;  // slot of this vertex in the caller's simplex
+};
+
+template <class T>
+struct Sx {
+  int n;
+  Vx<T> v[4];
+};
+
+template <class T>
+OGX_HD T tabs(T x) {
+  return x < T(0) ? -x : x;
+}
+
+// (p - q) . p > 0 : the origin projects beyond p towards q (openGJK.c:219-230)
+template <class T>
+OGX_HD bool edge_keeps(vec3<T> p, vec3<T> q, Unc& u) {
+  T acc = T(0);
+  acc += (p.x * p.x - p.x * q.x);
+  acc += (p.y * p.y - p.y * q.y);
+  acc += (p.z * p.z - p.z * q.z);
+  if (Eps<T>::v != 0.0) {
+    const T perm = p.x * p.x + tabs(p.x * q.x) + p.y * p.y + tabs(p.y * q.y) + p.z * p.z +
+                   tabs(p.z * q.z);
+    if (tabs(acc) <= T(16.0 * Eps<T>::v) * perm) u.hit = true;
+  }
+  return acc > T(0);
+}
+
+// origin beyond edge pq, away from r, in the plane pqr (openGJK.c:232-248)
+template <class T>
+OGX_HD bool edge_drops(vec3<T> p, vec3<T> q, vec3<T> r, Unc& u) {
+  const vec3<T> e1 = q - p, e2 = r - p;
+  const vec3<T> nrm = cross(e1, cross(e1, e2));
+  const T val = dot(p, nrm);
+  if (Eps<T>::v != 0.0) {
+    const T b = l1(e1);
+    if (tabs(val) <= T(64.0 * Eps<T>::v) * l1(p) * b * b * l1(e2)) u.hit = true;
+  }
+  return val < T(0);
+}
+
+// origin on the far side of triangle (p, q, r) seen from ... (openGJK.c:250-255)
+template <class T>
+OGX_HD bool face_drops(vec3<T> p, vec3<T> q, vec3<T> r, Unc& u) {
+  const T val = dot(p, cross(q, r));
+  if (Eps<T>::v != 0.0) {
+    if (tabs(val) <= T(32.0 * Eps<T>::v) * l1(p) * l1(q) * l1(r)) u.hit = true;
+  }
+  return val <= T(0);
+}
+
+template <class T>
+OGX_HD void onto_line(vec3<T> p, vec3<T> q, vec3<T>& out) {
+  const vec3<T> d = p - q;
+  const T t = dot(p, d) / dot(d, d);
+  out = p - d * t;
+}
+
+template <class T>
+OGX_HD void onto_plane(vec3<T> p, vec3<T> q, vec3<T> r, vec3<T>& out, Unc& u) {
+  const vec3<T> nrm = cross(p - q, p - r);
+  const T nn = dot(nrm, nrm);
+  if (Eps<T>::v != 0.0) {
+    const T b = T(32.0 * Eps<T>::v) * l1(p - q) * l1(p - r);
+    if (nn <= b * b) u.hit = true;
+  }
+  out = nrm * (dot(nrm, p) / nn);
+}
+
+template <class T>
+OGX_HD void keep1(Sx<T>& s, const Vx<T>& a) {
+  s.n = 1;
+  s.v[0] = a;
+}
+template <class T>
+OGX_HD void keep2(Sx<T>& s, const Vx<T>& a, const Vx<T>& b) {
+  s.n = 2;
+  s.v[0] = a;
+  s.v[1] = b;
+}
+template <class T>
+OGX_HD void keep3(Sx<T>& s, const Vx<T>& a, const Vx<T>& b, const Vx<T>& c) {
+  s.n = 3;
+  s.v[0] = a;
+  s.v[1] = b;
+  s.v[2] = c;
+}
+
+// segment: newest vertex v[1]
+template <class T>
+OGX_HD void sub_segment(Sx<T>& s, vec3<T>& dir, Unc& u) {
+  const Vx<T> q1 = s.v[1], q2 = s.v[0];
+  if (edge_keeps(q1.p, q2.p, u)) {
+    onto_line(q1.p, q2.p, dir);
+  } else {
+    dir = q1.p;
+    keep1(s, q1);
+  }
+}
+
+// triangle: newest vertex v[2]
+template <class T>
+OGX_HD void sub_triangle(Sx<T>& s, vec3<T>& dir, Unc& u) {
+  const Vx<T> q1 = s.v[2], q2 = s.v[1], q3 = s.v[0];
+  const bool k12 = edge_keeps(q1.p, q2.p, u);
+  const bool k13 = edge_keeps(q1.p, q3.p, u);
+  int pick = 0;  // 0 plane, 1 segment q1-q3, 2 segment q1-q2, 3 vertex q1
+  if (k12) {
+    if (!edge_drops(q1.p, q2.p, q3.p, u)) {
+      if (k13 && edge_drops(q1.p, q3.p, q2.p, u)) pick = 1;
+    } else {
+      pick = 2;
+    }
+  } else if (k13) {
+    if (edge_drops(q1.p, q3.p, q2.p, u)) pick = 1;
+  } else {
+    pick = 3;
+  }
+  if (pick == 0) {
+    onto_plane(q1.p, q2.p, q3.p, dir, u);
+  } else if (pick == 1) {
+    onto_line(q1.p, q3.p, dir);
+    keep2(s, q3, q1);
+  } else if (pick == 2) {
+    onto_line(q1.p, q2.p, dir);
+    keep2(s, q1, q2);
+  } else {
+    dir = q1.p;
+    keep1(s, q1);
+  }
+}
+
+// (k, i, j) naming of the three older tetrahedron vertices (openGJK.c:405-417)
+template <class T>
+OGX_HD void name_kij(int which, const Vx<T>& q2, const Vx<T>& q3, const Vx<T>& q4, Vx<T>& sk,
+                     Vx<T>& si, Vx<T>& sj) {
+  if (which == 0) {
+    sk = q2; si = q3; sj = q4;
+  } else if (which == 1) {
+    sk = q3; si = q4; sj = q2;
+  } else {
+    sk = q4; si = q2; sj = q3;
+  }
+}
+
+template <class T>
+OGX_HD void pick_plane(Sx<T>& s, const Vx<T>& a, const Vx<T>& b, const Vx<T>& q1,
+                       const vec3<T>& pp, const vec3<T>& pq, vec3<T>& dir, Unc& u) {
+  keep3(s, a, b, q1);
+  onto_plane(q1.p, pp, pq, dir, u);
+}
+template <class T>
+OGX_HD void pick_line(Sx<T>& s, const Vx<T>& a, const Vx<T>& q1, vec3<T>& dir) {
+  keep2(s, a, q1);
+  onto_line(q1.p, a.p, dir);
+}
+
+// tetrahedron: newest vertex v[3] (decision tree of openGJK.c:315-613)
+template <class T>
+OGX_HD void sub_tetra(Sx<T>& s, vec3<T>& dir, Unc& u) {
+  const Vx<T> q1 = s.v[3], q2 = s.v[2], q3 = s.v[1], q4 = s.v[0];
+  const bool l2 = edge_keeps(q1.p, q2.p, u);
+  const bool l3 = edge_keeps(q1.p, q3.p, u);
+  const bool l4 = edge_keeps(q1.p, q4.p, u);
+  const int nkeep = (int)l2 + (int)l3 + (int)l4;
+  if (nkeep == 0) {
+    dir = q1.p;
+    keep1(s, q1);
+    return;
+  }
+  const vec3<T> e2 = q2.p - q1.p, e3 = q3.p - q1.p, e4 = q4.p - q1.p;
+  const T vol = dot(e3, cross(e4, e2));
+  if (Eps<T>::v != 0.0) {
+    if (tabs(vol) <= T(32.0 * Eps<T>::v) * l1(e2) * l1(e3) * l1(e4)) u.hit = true;
+  }
+  const int neg = vol <= T(0);
+  int f2 = (int)face_drops(q1.p, q3.p, q4.p, u) - neg;
+  int f3 = (int)face_drops(q1.p, q4.p, q2.p, u) - neg;
+  int f4 = (int)face_drops(q1.p, q2.p, q3.p, u) - neg;
+  f2 *= f2;
+  f3 *= f3;
+  f4 *= f4;
+  Vx<T> sk, si, sj;
+  switch (f2 + f3 + f4) {
+    case 3:
+      dir = v3<T>(T(0), T(0), T(0));
+      return;
+    case 2:
+      if (!f2)
+        keep3(s, q4, q3, q1);
+      else if (!f3)
+        keep3(s, q4, q2, q1);
+      else
+        keep3(s, q3, q2, q1);
+      sub_triangle(s, dir, u);
+      return;
+    case 1: {
+      s.n = 3;
+      name_kij(f2 ? 0 : (f3 ? 1 : 2), q2, q3, q4, sk, si, sj);
+      const bool lk = edge_keeps(q1.p, sk.p, u);
+      const bool li = edge_keeps(q1.p, si.p, u);
+      const bool lj = edge_keeps(q1.p, sj.p, u);
+      if (nkeep == 1) {
+        if (lk) {
+          if (!edge_drops(q1.p, sk.p, si.p, u))
+            pick_plane(s, sk, si, q1, si.p, sk.p, dir, u);
+          else if (!edge_drops(q1.p, sk.p, sj.p, u))
+            pick_plane(s, sk, sj, q1, sj.p, sk.p, dir, u);
+          else
+            pick_line(s, sk, q1, dir);
+        } else if (li) {
+          if (!edge_drops(q1.p, si.p, sk.p, u))
+            pick_plane(s, sk, si, q1, si.p, sk.p, dir, u);
+          else
+            pick_line(s, si, q1, dir);
+        } else {
+          if (!edge_drops(q1.p, sj.p, sk.p, u))
+            pick_plane(s, sk, sj, q1, sj.p, sk.p, dir, u);
+          else
+            pick_line(s, sj, q1, dir);
+        }
+      } else if (nkeep == 2) {
+        if (li) {
+          if (!edge_drops(q1.p, sk.p, si.p, u)) {
+            if (!edge_drops(q1.p, si.p, sk.p, u))
+              pick_plane(s, sk, si, q1, si.p, sk.p, dir, u);
+            else
+              pick_line(s, sk, q1, dir);
+          } else if (!edge_drops(q1.p, sk.p, sj.p, u)) {
+            pick_plane(s, sk, sj, q1, sj.p, sk.p, dir, u);
+          } else {
+            pick_line(s, sk, q1, dir);
+          }
+        } else if (lj) {
+          if (!edge_drops(q1.p, sk.p, sj.p, u)) {
+            if (!edge_drops(q1.p, sj.p, sk.p, u))
+              pick_plane(s, sk, sj, q1, sj.p, sk.p, dir, u);
+            else
+              pick_line(s, sj, q1, dir);
+          } else if (!edge_drops(q1.p, sk.p, si.p, u)) {
+            pick_plane(s, sk, si, q1, si.p, sk.p, dir, u);
+          } else {
+            pick_line(s, sk, q1, dir);
+          }
+        } else {
+          u.hit = true;  // inconsistent tests: only possible through rounding
+        }
+      } else {
+        const bool d_ik = edge_drops(q1.p, si.p, sk.p, u);
+        const bool d_jk = edge_drops(q1.p, sj.p, sk.p, u);
+        const bool d_ki = edge_drops(q1.p, sk.p, si.p, u);
+        const bool d_kj = edge_drops(q1.p, sk.p, sj.p, u);
+        if (d_ki && d_kj)
+          pick_line(s, sk, q1, dir);
+        else if (d_ki) {
+          if (d_jk)
+            pick_line(s, sj, q1, dir);
+          else
+            pick_plane(s, sk, sj, q1, sk.p, sj.p, dir, u);
+        } else {
+          if (d_ik)
+            pick_line(s, si, q1, dir);
+          else
+            pick_plane(s, sk, si, q1, sk.p, si.p, dir, u);
+        }
+      }
+      return;
+    }
+    case 0:
+      if (nkeep == 1) {
+        name_kij(l3 ? 0 : (l4 ? 1 : 2), q2, q3, q4, sk, si, sj);
+        if (!edge_drops(q1.p, si.p, sj.p, u))
+          pick_plane(s, sj, si, q1, si.p, sj.p, dir, u);
+        else if (!edge_drops(q1.p, si.p, sk.p, u))
+          pick_plane(s, sk, si, q1, si.p, sk.p, dir, u);
+        else
+          pick_line(s, si, q1, dir);
+      } else if (nkeep == 2) {
+        s.n = 3;
+        name_kij(!l3 ? 0 : (!l4 ? 1 : 2), q2, q3, q4, sk, si, sj);
+        if (!edge_drops(q1.p, sj.p, sk.p, u)) {
+          if (!edge_drops(q1.p, sk.p, sj.p, u))
+            pick_plane(s, sk, sj, q1, sj.p, sk.p, dir, u);
+          else if (!edge_drops(q1.p, sk.p, si.p, u))
+            pick_plane(s, sk, si, q1, sk.p, si.p, dir, u);
+          else
+            pick_line(s, sk, q1, dir);
+        } else if (!edge_drops(q1.p, sj.p, si.p, u)) {
+          pick_plane(s, sj, si, q1, si.p, sj.p, dir, u);
+        } else {
+          pick_line(s, sj, q1, dir);
+        }
+      } else {
+        u.hit = true;  // all three edges keep but no face looks at the origin
+      }
+      return;
+    default:
+      return;
+  }
+}
+
+template <class T>
+OGX_HD void subdistance(Sx<T>& s, vec3<T>& dir, Unc& u) {
+  if (s.n == 4)
+    sub_tetra(s, dir, u);
+  else if (s.n == 3)
+    sub_triangle(s, dir, u);
+  else if (s.n == 2)
+    sub_segment(s, dir, u);
+}
+
+// --------------------------------------------------------------------------------
+// exact closest point of a simplex with <= 3 vertices to the origin, FP64
+// (region tests of Ericson, Real-Time Collision Detection, sec. 5.1.5, restated)
+
+OGX_HD void closest_on_simplex(int n, const dv3* P, double* lam, dv3& v) {
+  lam[0] = 1.0;
+  lam[1] = lam[2] = lam[3] = 0.0;
+  if (n == 1) {
+    v = P[0];
+    return;
+  }
+  if (n == 2) {
+    const dv3 e = P[1] - P[0];
+    const double ee = dot(e, e);
+    double t = ee > 0.0 ? -dot(P[0], e) / ee : 0.0;
+    t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+    lam[0] = 1.0 - t;
+    lam[1] = t;
+    v = P[0] + e * t;
+    return;
+  }
+  const dv3 a = P[0], b = P[1], c = P[2];
+  const dv3 ab = b - a, ac = c - a;
+  const double d1 = -dot(ab, a), d2 = -dot(ac, a);
+  if (d1 <= 0.0 && d2 <= 0.0) {
+    v = a;
+    return;
+  }
+  const double d3 = -dot(ab, b), d4 = -dot(ac, b);
+  if (d3 >= 0.0 && d4 <= d3) {
+    lam[0] = 0.0;
+    lam[1] = 1.0;
+    v = b;
+    return;
+  }
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
+    const double t = d1 / (d1 - d3);
+    lam[0] = 1.0 - t;
+    lam[1] = t;
+    v = a + ab * t;
+    return;
+  }
+  const double d5 = -dot(ab, c), d6 = -dot(ac, c);
+  if (d6 >= 0.0 && d5 <= d6) {
+    lam[0] = 0.0;
+    lam[2] = 1.0;
+    v = c;
+    return;
+  }
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
+    const double t = d2 / (d2 - d6);
+    lam[0] = 1.0 - t;
+    lam[2] = t;
+    v = a + ac * t;
+    return;
+  }
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
+    const double t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    lam[0] = 0.0;
+    lam[1] = 1.0 - t;
+    lam[2] = t;
+    v = b + (c - b) * t;
+    return;
+  }
+  const double den = 1.0 / (va + vb + vc);
+  const double s1 = vb * den, s2 = vc * den;
+  lam[0] = 1.0 - s1 - s2;
+  lam[1] = s1;
+  lam[2] = s2;
+  v = a + ab * s1 + ac * s2;
+}
+
+// --------------------------------------------------------------------------------
+// per-pair GJK
+
+struct GjkState {
+  int n;        // simplex size (4 = origin enclosed)
+  fv3 P[4];     // simplex Minkowski points, newest last
+  int ia[4], ib[4];
+  fv3 v;        // closest point of the simplex to the origin
+  float dist;
+  float wmax2;  // max |P|^2 seen (scale of the problem)
+  fv3 w0, w1;   // witnesses on body 1 and body 2
+  int iters;
+  int status;
+  bool polish;  // the FP32 distance is not known to polish_rel: re-solve in FP64
+};
+
+// The pair is in contact (EPA runs) when GJK enclosed the origin or the distance is
+// below FLT_EPSILON -- the reference's FP32 test (GJK/cpu/EPA.c:370).
+OGX_HD bool gjk_contact(const GjkState& g) { return g.n == 4 || !(g.dist > FLT_EPSILON); }
+
+// barycentric weights of the closest point v of the final simplex, FP32
+OGX_HD void simplex_weights(const GjkState& g, float* lam) {
+  lam[0] = 1.0f;
+  lam[1] = lam[2] = lam[3] = 0.0f;
+  if (g.n == 2) {
+    const fv3 e = g.P[1] - g.P[0];
+    const float ee = dot(e, e);
+    float t = ee > 0.0f ? -dot(g.P[0], e) / ee : 0.0f;
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    lam[0] = 1.0f - t;
+    lam[1] = t;
+  } else if (g.n == 3) {
+    const fv3 e1 = g.P[1] - g.P[0], e2 = g.P[2] - g.P[0];
+    const float g11 = dot(e1, e1), g12 = dot(e1, e2), g22 = dot(e2, e2);
+    const float r1 = -dot(g.P[0], e1), r2 = -dot(g.P[0], e2);
+    const float det = g11 * g22 - g12 * g12;
+    if (det != 0.0f) {
+      const float a1 = (g22 * r1 - g12 * r2) / det;
+      const float a2 = (g11 * r2 - g12 * r1) / det;
+      lam[0] = 1.0f - a1 - a2;
+      lam[1] = a1;
+      lam[2] = a2;
+    }
+  } else if (g.n == 4) {
+    const fv3 e1 = g.P[1] - g.P[0], e2 = g.P[2] - g.P[0], e3 = g.P[3] - g.P[0];
+    const fv3 c23 = cross(e2, e3), c31 = cross(e3, e1), c12 = cross(e1, e2);
+    const float det = dot(e1, c23);
+    if (det != 0.0f) {
+      const fv3 o = -g.P[0];
+      const float a1 = dot(o, c23) / det, a2 = dot(o, c31) / det, a3 = dot(o, c12) / det;
+      lam[0] = 1.0f - a1 - a2 - a3;
+      lam[1] = a1;
+      lam[2] = a2;
+      lam[3] = a3;
+    }
+  }
+}
+
+template <class Team, class Bodies>
+OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g) {
+  const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
+  const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
+  const fv3 a0 = B.point(0, 0), b0 = B.point(1, 0);
+  fv3 v = a0 - b0;
+  g.n = 1;
+  g.P[0] = v;
+  g.ia[0] = 0;
+  g.ib[0] = 0;
+  g.status = 0;
+  g.wmax2 = 0.0f;
+  fv3 sa = a0, sb = b0;
+  int ia = 0, ib = 0;
+  const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
+  const float contact = reftol ? cfg.gjk_eps_tot : cfg.gjk_noise * FLT_EPSILON;
+  int k = 0;
+  for (;;) {
+    ++k;
+    const fv3 mv = -v;
+    float ba, bb;
+    int xa, xb;
+    B.scan(t, 0, mv, ba, xa);
+    B.scan(t, 1, v, bb, xb);
+    t.argmax(ba, xa);
+    t.argmax(bb, xb);
+    if (ba > sdot(sa, mv)) {
+      ia = xa;
+      sa = B.point(0, xa);
+    }
+    if (bb > sdot(sb, v)) {
+      ib = xb;
+      sb = B.point(1, xb);
+    }
+    const fv3 w = sa - sb;
+    const float vv = dot(v, v);
+    const float gap = vv - dot(v, w);
+    float floor_ = cfg.gjk_eps_tot;
+    if (!reftol) {
+      const float nv = sqrtf(vv);
+      floor_ = fmaxf(floor_, cfg.gjk_noise * FLT_EPSILON * nv * (nv + sqrtf(dot(w, w))));
+    }
+    if (gap <= cfg.gjk_eps_rel * vv || gap < floor_) break;
+    if (vv < eps_rel2) break;
+    if (!reftol) {
+      bool dup = false;
+      for (int j = 0; j < g.n; ++j) dup |= (g.ia[j] == ia && g.ib[j] == ib);
+      if (dup) break;
+    }
+    g.P[g.n] = w;
+    g.ia[g.n] = ia;
+    g.ib[g.n] = ib;
+    g.n++;
+
+    Sx<float> sf;
+    sf.n = g.n;
+    for (int j = 0; j < g.n; ++j) {
+      sf.v[j].p = g.P[j];
+      sf.v[j].k = j;
+    }
+    Unc u{false};
+    fv3 nvf = v;
+    subdistance(sf, nvf, u);
+    int order[4] = {0, 1, 2, 3};
+    int nn = sf.n;
+    if (u.hit && escalate) {
+      Sx<double> sd;
+      sd.n = g.n;
+      for (int j = 0; j < g.n; ++j) {
+        sd.v[j].p = B.dpoint(0, g.ia[j]) - B.dpoint(1, g.ib[j]);
+        sd.v[j].k = j;
+      }
+      dv3 vd = cvt<double>(v);
+      Unc ud{false};
+      subdistance(sd, vd, ud);
+      nn = sd.n;
+      for (int j = 0; j < nn; ++j) order[j] = sd.v[j].k;
+      v = cvt<float>(vd);
+      g.status |= OGX_S_GJK_ESCALATED;
+    } else {
+      for (int j = 0; j < nn; ++j) order[j] = sf.v[j].k;
+      v = nvf;
+    }
+    {
+      fv3 P2[4];
+      int a2[4], b2[4];
+      for (int j = 0; j < nn; ++j) {
+        P2[j] = g.P[order[j]];
+        a2[j] = g.ia[order[j]];
+        b2[j] = g.ib[order[j]];
+      }
+      for (int j = 0; j < nn; ++j) {
+        g.P[j] = P2[j];
+        g.ia[j] = a2[j];
+        g.ib[j] = b2[j];
+      }
+      g.n = nn;
+    }
+    for (int j = 0; j < g.n; ++j) g.wmax2 = fmaxf(g.wmax2, dot(g.P[j], g.P[j]));
+    if (dot(v, v) <= contact * contact * g.wmax2) break;
+    if (g.n == 4 || k == cfg.gjk_max_iter) break;
+  }
+  if (k == cfg.gjk_max_iter && g.n != 4) g.status |= OGX_S_GJK_CAP;
+  g.iters = k;
+  g.v = v;
+  g.dist = sqrtf(dot(v, v));
+
+  float lam[4];
+  simplex_weights(g, lam);
+  fv3 w0 = v3<float>(0.f, 0.f, 0.f), w1 = w0;
+  for (int j = 0; j < g.n; ++j) {
+    w0 = w0 + B.point(0, g.ia[j]) * lam[j];
+    w1 = w1 + B.point(1, g.ib[j]) * lam[j];
+  }
+  g.w0 = w0;
+  g.w1 = w1;
+
+  // FP32 error of |v| is a few ulp of the simplex scale; ask for an FP64 re-solve when
+  // that is not small against the distance.
+  g.polish = false;
+  if ((cfg.flags & OGX_F_FP64_POLISH) && g.n >= 2 && g.n <= 3 && !gjk_contact(g)) {
+    const float errb = 16.0f * FLT_EPSILON * sqrtf(g.wmax2);
+    g.polish = errb > cfg.polish_rel * g.dist;
+  }
+}
+
+// FP64 re-solve of the final simplex: exact Minkowski points, exact closest point.
+template <class Bodies>
+OGX_HD void gjk_polish(const Bodies& B, GjkState& g) {
+  dv3 P[3];
+  for (int j = 0; j < g.n && j < 3; ++j) P[j] = B.dpoint(0, g.ia[j]) - B.dpoint(1, g.ib[j]);
+  double lam[4];
+  dv3 v;
+  closest_on_simplex(g.n, P, lam, v);
+  dv3 w0 = v3<double>(0.0, 0.0, 0.0), w1 = w0;
+  for (int j = 0; j < g.n; ++j) {
+    w0 = w0 + B.dpoint(0, g.ia[j]) * lam[j];
+    w1 = w1 + B.dpoint(1, g.ib[j]) * lam[j];
+  }
+  g.v = cvt<float>(v);
+  g.dist = (float)sqrt(dot(v, v));
+  g.w0 = cvt<float>(w0);
+  g.w1 = cvt<float>(w1);
+  g.status |= OGX_S_POLISHED;
+}
+
+}  // namespace ogx

@@ -1,0 +1,129 @@
+// ogx_twin.cpp -- TEST BUILD ONLY.  Runs the engine's per-pair GJK/EPA code (the same
+// __host__ __device__ source the CUDA kernels instantiate) on the CPU with a one-lane
+// team, so the algorithm can be checked against the oracle on a machine without a GPU
+// and GPU results can be compared with the identical arithmetic on the host.  The
+// product library never contains this file.
+#include <pthread.h>
+#include <string.h>
+
+#include <vector>
+
+#include "ogx_bodies.cuh"
+#include "ogx_epa.cuh"
+#include "ogx_gjk.cuh"
+
+using namespace ogx;
+
+namespace {
+
+struct Job {
+  int lo, hi, mode;
+  const float* pool;
+  const uint32_t* quad;
+  const int32_t* counts;
+  const int32_t* pairs;
+  const ogx_config* cfg;
+  float* dist;
+  gkSimplex* smp;
+  float* nrm;
+  int32_t* status;
+  int32_t* iters;
+};
+
+void one(const Job& J, int i, EpaMem& M) {
+  const int b1 = J.pairs[2 * i], b2 = J.pairs[2 * i + 1];
+  BodyRef A{J.quad[b1], J.counts[b1]}, Bb{J.quad[b2], J.counts[b2]};
+  MemBodies B;
+  B.bind(J.pool, A, Bb);
+  SerialTeam t;
+  GjkState g;
+  gjk_pair(t, B, *J.cfg, g);
+  // same order as the device pipeline: the contact decision is taken on the FP32 GJK
+  // result, separated pairs are then re-solved in FP64, contacts go through EPA
+  const bool contact = gjk_contact(g);
+  if (g.polish) gjk_polish(B, g);
+  gkSimplex& s = J.smp[i];
+  s.nvrtx = g.n;
+  for (int k = 0; k < 4; ++k) {
+    const bool live = k < g.n;
+    s.vrtx[k][0] = live ? g.P[k].x : 0.f;
+    s.vrtx[k][1] = live ? g.P[k].y : 0.f;
+    s.vrtx[k][2] = live ? g.P[k].z : 0.f;
+    s.vrtx_idx[k][0] = live ? g.ia[k] : 0;
+    s.vrtx_idx[k][1] = live ? g.ib[k] : 0;
+  }
+  float d = g.dist;
+  fv3 w0 = g.w0, w1 = g.w1, n = v3<float>(0.f, 0.f, 0.f);
+  int st = g.status, ei = 0;
+  if (J.mode == 2) {
+    if (contact) {
+      EpaOut o;
+      epa_pair(t, B, *J.cfg, g, M, o);
+      if (o.polish) epa_polish(B, o);
+      d = o.dist;
+      w0 = o.w0;
+      w1 = o.w1;
+      n = o.nrm;
+      st |= o.status;
+      ei = o.iters;
+    } else {
+      n = unit_or_x(w1 - w0);
+    }
+  }
+  J.dist[i] = d;
+  s.witnesses[0][0] = w0.x;
+  s.witnesses[0][1] = w0.y;
+  s.witnesses[0][2] = w0.z;
+  s.witnesses[1][0] = w1.x;
+  s.witnesses[1][1] = w1.y;
+  s.witnesses[1][2] = w1.z;
+  if (J.nrm) {
+    J.nrm[3 * i] = n.x;
+    J.nrm[3 * i + 1] = n.y;
+    J.nrm[3 * i + 2] = n.z;
+  }
+  if (J.status) J.status[i] = st;
+  if (J.iters) {
+    J.iters[2 * i] = g.iters;
+    J.iters[2 * i + 1] = ei;
+  }
+}
+
+void* worker(void* arg) {
+  const Job& J = *static_cast<const Job*>(arg);
+  EpaMem* M = new EpaMem;
+  for (int i = J.lo; i < J.hi; ++i) one(J, i, *M);
+  delete M;
+  return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+int twin_config(int reference, ogx_config* out) {
+  *out = reference ? reference_config() : default_config();
+  return 0;
+}
+
+int twin_run(int npairs, const float* pool, const uint32_t* quad, const int32_t* counts,
+             const int32_t* pairs, int mode, const ogx_config* cfg, float* dist, gkSimplex* smp,
+             float* nrm, int32_t* status, int32_t* iters, int nthreads) {
+  if (npairs < 0 || (mode != 1 && mode != 2)) return -1;
+  Job base{0, npairs, mode, pool, quad, counts, pairs, cfg, dist, smp, nrm, status, iters};
+  if (nthreads <= 1 || npairs < 64) {
+    worker(&base);
+    return 0;
+  }
+  if (nthreads > 64) nthreads = 64;
+  std::vector<pthread_t> th(nthreads);
+  std::vector<Job> jobs(nthreads, base);
+  for (int k = 0; k < nthreads; ++k) {
+    jobs[k].lo = (int)((int64_t)npairs * k / nthreads);
+    jobs[k].hi = (int)((int64_t)npairs * (k + 1) / nthreads);
+    pthread_create(&th[k], nullptr, worker, &jobs[k]);
+  }
+  for (int k = 0; k < nthreads; ++k) pthread_join(th[k], nullptr);
+  return 0;
+}
+}
