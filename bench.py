@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark: batched GJK+EPA pairs/s on one GB300 (FP32 bulk, FP64 where needed).
+
+Workload (default): 1,000,000 pairs in one batch; vertex counts from a discrete power
+law p(n) ~ n^-1.5 on [4, 1024]; points uniform on random ellipsoids (semi-axes
+U[0.3, 2], uniform rotation); centres placed so that about half the pairs overlap.
+Seeded synthetic data (no dataset exists for this benchmark).
+
+One step = one pass of the whole pipeline (bin, GJK, EPA on the contacts, FP64 polish)
+over the batch.  `value` is measured with inputs resident in HBM (the pool is 1.5 GB,
+larger than L2, so no flush is needed between steps); `e2e` repeats the step through
+the C ABI with host buffers: pinned host points + pairs copied in, results copied out.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "opengjk-gpu_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "GJK+EPA pairs/s on 1 GB300 (FP32, <=1e-5 rel err)"
+WORKLOADS = {
+    "powerlaw": dict(desc="GJK+EPA, 1,000,000 pairs, power-law vertex counts on [4,1024] (exp -1.5), "
+                          "ellipsoid point sets, ~50% overlapping", n_pairs=1_000_000),
+    "ellipsoid": dict(desc="GJK+EPA, 100,000 pairs, log-uniform vertex counts on [8,256], "
+                           "ellipsoid point sets, ~50% overlapping", n_pairs=100_000),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="powerlaw", choices=sorted(WORKLOADS))
+    ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-launches", action="store_true",
+                    help="one untimed step only (for ncu launch lists)")
+    return ap.parse_args()
+
+
+def make_batch(name: str, n_pairs: int, seed: int):
+    from ogx import workloads as W
+    if name == "powerlaw":
+        return W.powerlaw(seed=seed, n_pairs=n_pairs)
+    return W.ellipsoid(seed=seed, n_pairs=n_pairs)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if r.returncode == 0 and r.stdout.strip():
+                    self.samples.append([x.strip() for x in r.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if len(s) > 3 + k and s[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
+    """Reference CPU GJK+EPA on the host cores (all threads), on a bounded sample of the
+    same workload: the reference's own CPU build when present, else the oracle port."""
+    from oracle import orc
+    threads = os.cpu_count() or 1
+    use_ref = orc.ref_available()
+    kind = "reference" if use_ref else "port"
+    m = orc.MODE_GJK_EPA
+    # calibrate the sample size on a small slice
+    n0 = min(batch.n_pairs, 4000)
+    sub = batch.subset(np.arange(n0))
+    t = time.perf_counter()
+    _cpu_run(orc, sub, m, threads, use_ref)
+    per_pair = max((time.perf_counter() - t) / n0, 1e-9)
+    n = int(min(batch.n_pairs, max(n0, seconds / per_pair)))
+    sub = batch.subset(np.arange(n))
+    t = time.perf_counter()
+    _cpu_run(orc, sub, m, threads, use_ref)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": "pairs/s", "cores": threads if not use_ref else threads,
+            "kind": kind, "sample": f"first {n} pairs of the workload, FP32 reference tolerances, "
+                                   f"{threads} threads, {dt:.1f} s"}
+
+
+def _cpu_run(orc, b, mode, threads, use_ref):
+    if use_ref:
+        # the reference's own per-pair functions, pair ranges over host threads
+        import concurrent.futures as cf
+        chunks = np.array_split(np.arange(b.n_pairs), threads)
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(lambda c: orc.run_reference(b.coords, b.offsets, b.counts, b.pairs[c], mode=mode,
+                                                    precision="f32"), chunks))
+    else:
+        orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=mode, precision="f32", threads=threads)
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    spec = WORKLOADS[args.workload]
+    n = args.pairs or spec["n_pairs"]
+    batch = make_batch(args.workload, n, seed=1000)
+    from oracle import orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    use_ref = orc.ref_available()
+    # each step: a bounded sample (~4 s of CPU work) of the same workload
+    n0 = min(n, 4000)
+    t = time.perf_counter()
+    _cpu_run(orc, batch.subset(np.arange(n0)), orc.MODE_GJK_EPA, threads, use_ref)
+    per_pair = (time.perf_counter() - t) / n0
+    ns = int(min(n, max(n0, 4.0 / max(per_pair, 1e-9))))
+    sample = batch.subset(np.arange(ns))
+    for _ in range(args.warmup):
+        _cpu_run(orc, sample.subset(np.arange(min(ns, 2000))), orc.MODE_GJK_EPA, threads, use_ref)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        _cpu_run(orc, sample, orc.MODE_GJK_EPA, threads, use_ref)
+        times.append(time.perf_counter() - t)
+    ms = 1e3 * statistics.mean(times)
+    value = ns / (ms / 1e3)
+    kind = "reference" if use_ref else "port"
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": spec["desc"], "pairs_per_step": ns, "sample_of": n},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind,
+                         "sample": f"first {ns} of {n} pairs per step, {threads} host threads"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from ogx import build, engine, _lib
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    build.build()
+    spec = WORKLOADS[args.workload]
+    n = args.pairs or spec["n_pairs"]
+    batch = make_batch(args.workload, n, seed=1000 + rank)   # weak scaling: own shard per rank
+    alg_bytes = batch.algorithmic_bytes(with_epa=True)
+    stream = torch.cuda.Stream()
+    ctx = engine.Context(local, stream=stream)
+    pool = engine.Pool(ctx, batch.counts)
+    coords_pinned = torch.from_numpy(batch.coords).pin_memory()
+    pairs_pinned = torch.from_numpy(np.ascontiguousarray(batch.pairs)).pin_memory()
+    pool.upload(coords_pinned)
+    pairs = pairs_pinned.to(f"cuda:{local}", non_blocking=True)
+    out = engine.Results(n, pairs.device)
+    torch.cuda.synchronize()
+
+    # one instrumented step: per-kernel CUDA-event times and work counts
+    ctx.set_timing(True)
+    with torch.cuda.stream(stream):
+        engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+    ktimes = ctx.kernel_times()
+    counts = ctx.work_counts()
+    ctx.set_timing(False)
+    if args.profile_launches:
+        torch.cuda.synchronize()
+        return
+
+    for _ in range(args.warmup):
+        engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+    launches_per_step = ctx.last_launches
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms / 1e3)
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        host_out = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory()
+                    for k, v in (("simplex", out.simplex), ("dist", out.dist), ("normal", out.normal),
+                                 ("status", out.status))}
+        d2h = sum(t.numel() * t.element_size() for t in host_out.values())
+        h2d = coords_pinned.numel() * 4 + pairs_pinned.numel() * 4
+        e2e_steps = max(3, min(args.steps, 10))
+
+        def e2e_step():
+            with torch.cuda.stream(stream):
+                pool.upload(coords_pinned)
+                pairs.copy_(pairs_pinned, non_blocking=True)
+                engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+                host_out["simplex"].copy_(out.simplex, non_blocking=True)
+                host_out["dist"].copy_(out.dist, non_blocking=True)
+                host_out["normal"].copy_(out.normal, non_blocking=True)
+                host_out["status"].copy_(out.status, non_blocking=True)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = e0.elapsed_time(e1) / e2e_steps
+        if world > 1:
+            t = torch.tensor([ems], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ems = float(t.item())
+        e2e = {"value": world * n / (ems / 1e3), "unit": "pairs/s", "ms_per_step": ems,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "path": "ogx_pool_upload + ogx_gjk_epa + result copies, pinned host buffers"}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # roofline of the dominant kernel
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    tot = sum(t for _, t in ktimes)
+    dom_name, dom_ms = max(ktimes, key=lambda kv: kv[1])
+    from ogx.workloads import Batch  # noqa: F401
+    nv = batch.pair_vertex_counts()
+    m = np.maximum(batch.counts[batch.pairs[:, 0]], batch.counts[batch.pairs[:, 1]])
+    edges = [0, 16, 32, 64, 128, 256, 512, 1 << 30]
+    bucket = np.searchsorted(edges, m, side="left") - 1
+    kind, lab = dom_name.split("<=")[0].split(">")[0], dom_name
+    bi = ["<=16", "<=32", "<=64", "<=128", "<=256", "<=512", ">512"]
+    b_id = [i for i, s in enumerate(bi) if dom_name.endswith(s)]
+    if b_id and kind == "gjk":
+        sel = bucket == b_id[0]
+        dom_bytes = int(12 * nv[sel].sum() + 120 * sel.sum())
+    elif b_id and kind == "epa":
+        # contacts of the bucket: their points plus the EPA outputs (depth, witnesses, normal)
+        frac = counts["epa"][b_id[0]] / max(1, counts["gjk"][b_id[0]])
+        sel = bucket == b_id[0]
+        dom_bytes = int(frac * (12 * nv[sel].sum() + 8 * sel.sum()) + 40 * counts["epa"][b_id[0]])
+    else:
+        dom_bytes = int(alg_bytes)
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    pipeline_gbs = alg_bytes / (ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+            "kernel_share": dom_ms / tot if tot else None,
+            "pipeline_achieved": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak,
+            "algorithmic_bytes_per_step": int(alg_bytes)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": spec["desc"], "pairs_per_gpu": n, "mean_vertices_per_body":
+                   float(batch.counts.mean()), "l2": "inputs (pool %.2f GB) larger than L2, no flush"
+                   % (batch.coords.nbytes / 1e9), "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk.summary(),
+        "roofline": roof,
+        "kernels_ms": {k: round(v, 4) for k, v in ktimes},
+        "work": counts,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(batch)
+    print(json.dumps(line), flush=True)
+    pool.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -130,6 +130,15 @@ ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkColli
 
 /* Kernels launched by the last engine call on this context (for accounting). */
 int ogx_ctx_last_launches(const ogx_ctx* ctx);
+/* Per-launch timing: when on, each batched call records CUDA events on the context's
+ * stream between its launches.  ogx_ctx_kernel_times waits for the last call and
+ * fills up to cap (name, milliseconds) entries; returns the number filled. */
+ogx_status ogx_ctx_set_timing(ogx_ctx* ctx, int on);
+int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
+/* Work counts of the last call (waits for it): pairs per GJK bucket [0, 7), contacts
+ * per EPA bucket [7, 14), EPA faces re-solved in FP64 [14], pairs whose GJK result was
+ * refined in FP64 [15].  cap must be >= 16. */
+int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 #ifdef __cplusplus
 }

@@ -32,6 +32,7 @@ struct MemBodies {
     return v3<float>(p[i], p[n4[w] + i], p[2 * n4[w] + i]);
   }
   OGX_HD dv3 dpoint(int w, int i) const { return cvt<double>(point(w, i)); }
+  OGX_HD const MemBodies& mem_view() const { return *this; }
 
   template <class Team>
   OGX_HD void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {
@@ -89,6 +90,7 @@ struct RegBodies {
   }
   __device__ fv3 point(int w, int i) const { return mem.point(w, i); }
   __device__ dv3 dpoint(int w, int i) const { return mem.dpoint(w, i); }
+  __device__ const MemBodies& mem_view() const { return mem; }
 
   template <class Team>
   __device__ void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {

@@ -1,0 +1,559 @@
+// ogx_engine.cu -- engine half of the C ABI (include/ogx.h): contexts, the device-
+// resident polytope pool, and the batched GJK / GJK+EPA / EPA pipelines.
+//
+// Pipeline of one batched call (all on the context's stream, no host synchronisation):
+//   memset counters -> k_bin -> k_gjk x 7 buckets (largest first) -> k_epa x 7 ->
+//   k_polish
+// Grids are fixed per kernel (occupancy x SM count) and the kernels stride over
+// device-side work lists, so a call is a fixed sequence of launches that can be
+// captured in a CUDA graph by the caller.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "ogx_engine.h"
+
+using namespace ogx;
+
+// ---------------------------------------------------------------------------------
+// errors
+
+static thread_local std::string g_err;
+
+ogx_status ogx_fail(ogx_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return s;
+}
+
+ogx_status ogx_cuda_fail(cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a non-sticky error
+  const ogx_status s = (e == cudaErrorMemoryAllocation) ? OGX_ERR_NOMEM : OGX_ERR_CUDA;
+  return ogx_fail(s, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+extern "C" const char* ogx_last_error(void) { return g_err.c_str(); }
+
+extern "C" const char* ogx_status_string(ogx_status s) {
+  switch (s) {
+    case OGX_OK: return "ok";
+    case OGX_ERR_INVALID: return "invalid argument";
+    case OGX_ERR_CUDA: return "CUDA error";
+    case OGX_ERR_NOMEM: return "out of memory";
+    case OGX_ERR_NO_DEVICE: return "no usable GPU";
+    case OGX_ERR_CAPACITY: return "capacity exceeded";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char* ogx_version(void) { return "ogx 0.1 (sm_103a)"; }
+
+extern "C" ogx_status ogx_config_default(ogx_config* cfg) {
+  if (!cfg) return ogx_fail(OGX_ERR_INVALID, "cfg is NULL");
+  *cfg = default_config();
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_config_reference(ogx_config* cfg) {
+  if (!cfg) return ogx_fail(OGX_ERR_INVALID, "cfg is NULL");
+  *cfg = reference_config();
+  return OGX_OK;
+}
+
+static ogx_status check_config(const ogx_config& c) {
+  if (!(c.gjk_max_iter >= 1 && c.gjk_max_iter <= 1000))
+    return ogx_fail(OGX_ERR_INVALID, "gjk_max_iter must be in [1, 1000]");
+  if (!(c.epa_max_iter >= 1 && c.epa_max_iter <= kEpaVmax - 4))
+    return ogx_fail(OGX_ERR_INVALID, "epa_max_iter must be in [1, %d]", kEpaVmax - 4);
+  if (!(c.gjk_eps_rel >= 0.f) || !(c.gjk_eps_tot >= 0.f) || !(c.epa_tol >= 0.f) ||
+      !(c.epa_rel >= 0.f) || !(c.epa_vis >= 0.f) || !(c.gjk_noise >= 0.f) || !(c.polish_rel >= 0.f))
+    return ogx_fail(OGX_ERR_INVALID, "tolerances must be >= 0");
+  return OGX_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// kernel table
+
+namespace {
+
+struct Launch {
+  BucketKernel fn;
+  int L;
+  size_t smem;
+  int grid;  // resident blocks x SMs on the current device
+};
+
+Launch g_gjk[kBuckets];
+Launch g_epa[kBuckets];
+
+constexpr int kBlock = 128;
+
+std::mutex g_init_mu;
+int g_init_device = -1;
+int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0;
+
+ogx_status init_kernels(int device) {
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (g_init_device == device) return OGX_OK;
+  int sms = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaDeviceGetAttribute");
+  for (int b = 0; b < kBuckets; ++b) {
+    g_gjk[b] = Launch{gjk_kernels()[b].fn, gjk_kernels()[b].L, 0, 0};
+    g_epa[b] = Launch{epa_kernels()[b].fn, epa_kernels()[b].L, 0, 0};
+    for (Launch* k : {&g_gjk[b], &g_epa[b]}) {
+      const bool epa = (k == &g_epa[b]);
+      k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMem) : 0;
+      if (k->smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn),
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k->smem);
+        if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaFuncSetAttribute");
+      }
+      int per_sm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->fn, kBlock, k->smem);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      if (per_sm < 1) return ogx_fail(OGX_ERR_CUDA, "bucket kernel %d cannot be resident", b);
+      k->grid = per_sm * sms;
+    }
+  }
+  g_grid_bin = 4 * sms;
+  g_grid_pack = 8 * sms;
+  int per_sm = 0;
+  e = polish_occupancy(kBlock, &per_sm);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy(k_polish)");
+  g_grid_polish = std::max(1, per_sm) * sms;
+  e = refine_occupancy(kBlock, &per_sm);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy(k_refine)");
+  g_grid_refine = std::max(1, per_sm) * sms;
+  g_init_device = device;
+  return OGX_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// context
+
+extern "C" ogx_status ogx_ctx_create(int device, const ogx_config* cfg, void* stream,
+                                     ogx_ctx** out) {
+  if (!out) return ogx_fail(OGX_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return ogx_fail(OGX_ERR_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+  }
+  if (device < 0) {
+    e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaGetDevice");
+  }
+  if (device >= ndev) return ogx_fail(OGX_ERR_INVALID, "device %d of %d", device, ndev);
+  int major = 0, minor = 0;
+  cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+  if (major * 10 + minor != 103)
+    return ogx_fail(OGX_ERR_NO_DEVICE, "device %d is sm_%d%d; this build is sm_103a only", device,
+                    major, minor);
+  ogx_config c = cfg ? *cfg : default_config();
+  ogx_status s = check_config(c);
+  if (s) return s;
+  e = cudaSetDevice(device);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaSetDevice");
+  s = init_kernels(device);
+  if (s) return s;
+  ogx_ctx* ctx = new ogx_ctx();
+  ctx->device = device;
+  ctx->cfg = c;
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (stream) {
+    ctx->stream = static_cast<cudaStream_t>(stream);
+    ctx->own_stream = false;
+  } else {
+    e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete ctx;
+      return ogx_cuda_fail(e, "cudaStreamCreate");
+    }
+    ctx->own_stream = true;
+  }
+  *out = ctx;
+  return OGX_OK;
+}
+
+void ogx_ctx::free_scratch() {
+  cudaFree(d_lists);
+  cudaFree(d_elists);
+  cudaFree(d_polish);
+  cudaFree(d_counts);
+  cudaFree(d_refine);
+  d_refine = nullptr;
+  d_lists = d_elists = d_counts = nullptr;
+  d_polish = nullptr;
+  cap_pairs = 0;
+}
+
+extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
+  if (!ctx) return OGX_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->free_scratch();
+  for (int i = 0; i <= ogx_ctx::kMaxTimed; ++i)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
+  if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_ctx_set_config(ogx_ctx* ctx, const ogx_config* cfg) {
+  if (!ctx || !cfg) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  ogx_status s = check_config(*cfg);
+  if (s) return s;
+  ctx->cfg = *cfg;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_ctx_get_config(const ogx_ctx* ctx, ogx_config* cfg) {
+  if (!ctx || !cfg) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  *cfg = ctx->cfg;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_ctx_set_stream(ogx_ctx* ctx, void* stream) {
+  if (!ctx) return ogx_fail(OGX_ERR_INVALID, "ctx is NULL");
+  if (ctx->own_stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+  }
+  ctx->stream = static_cast<cudaStream_t>(stream);
+  return OGX_OK;
+}
+
+extern "C" void* ogx_ctx_stream(const ogx_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+extern "C" ogx_status ogx_ctx_synchronize(ogx_ctx* ctx) {
+  if (!ctx) return ogx_fail(OGX_ERR_INVALID, "ctx is NULL");
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaStreamSynchronize");
+  return OGX_OK;
+}
+
+extern "C" int ogx_ctx_last_launches(const ogx_ctx* ctx) { return ctx ? ctx->last_launches : 0; }
+
+void ogx_ctx::mark(const char* name) {
+  if (!timing || ev_count >= kMaxTimed) return;
+  cudaEventRecord(ev[ev_count], stream);
+  ev_name[ev_count] = name;
+  ++ev_count;
+}
+
+extern "C" ogx_status ogx_ctx_set_timing(ogx_ctx* ctx, int on) {
+  if (!ctx) return ogx_fail(OGX_ERR_INVALID, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  if (on && !ctx->ev[0]) {
+    for (int i = 0; i <= ogx_ctx::kMaxTimed; ++i) {
+      cudaError_t e = cudaEventCreate(&ctx->ev[i]);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaEventCreate");
+    }
+  }
+  ctx->timing = on != 0;
+  return OGX_OK;
+}
+
+extern "C" int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap) {
+  if (!ctx || !ctx->timing || ctx->ev_count == 0) return 0;
+  if (cudaEventSynchronize(ctx->ev[ctx->ev_count]) != cudaSuccess) return -1;
+  const int n = std::min(cap, ctx->ev_count);
+  for (int i = 0; i < n; ++i) {
+    if (names) names[i] = ctx->ev_name[i];
+    if (ms) cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]);
+  }
+  return n;
+}
+
+extern "C" int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap) {
+  if (!ctx || !ctx->d_counts || cap < kCntSlots) return 0;
+  if (cudaMemcpyAsync(counts, ctx->d_counts, kCntSlots * sizeof(int), cudaMemcpyDeviceToHost,
+                      ctx->stream) != cudaSuccess ||
+      cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+    return -1;
+  return kCntSlots;
+}
+
+ogx_status ogx_ctx::ensure_scratch(int npairs) {
+  if ((size_t)npairs <= cap_pairs && d_counts) return OGX_OK;
+  cudaStreamSynchronize(stream);
+  free_scratch();
+  size_t cap = std::max<size_t>(1024, (size_t)npairs + npairs / 4);
+  cudaError_t e;
+  if ((e = cudaMalloc(&d_lists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_elists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_polish, cap * sizeof(PolishRec))) != cudaSuccess ||
+      (e = cudaMalloc(&d_refine, cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_counts, 64 * sizeof(int))) != cudaSuccess) {
+    free_scratch();
+    return ogx_cuda_fail(e, "scratch allocation");
+  }
+  cap_pairs = cap;
+  return OGX_OK;
+}
+
+ogx_status ogx_ctx::ensure_stage(size_t host_bytes, size_t dev_bytes) {
+  cudaError_t e;
+  if (host_bytes > h_stage_bytes) {
+    cudaStreamSynchronize(stream);
+    if (h_stage) cudaFreeHost(h_stage);
+    h_stage = nullptr;
+    h_stage_bytes = 0;
+    if ((e = cudaMallocHost(&h_stage, host_bytes)) != cudaSuccess)
+      return ogx_cuda_fail(e, "pinned staging allocation");
+    h_stage_bytes = host_bytes;
+  }
+  if (dev_bytes > d_stage_bytes) {
+    cudaStreamSynchronize(stream);
+    if (d_stage) cudaFree(d_stage);
+    d_stage = nullptr;
+    d_stage_bytes = 0;
+    if ((e = cudaMalloc(&d_stage, dev_bytes)) != cudaSuccess)
+      return ogx_cuda_fail(e, "device staging allocation");
+    d_stage_bytes = dev_bytes;
+  }
+  return OGX_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// pool
+
+extern "C" ogx_status ogx_pool_create(ogx_ctx* ctx, int num_bodies, const int32_t* counts,
+                                      ogx_pool** out) {
+  if (!ctx || !out || (!counts && num_bodies > 0))
+    return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  if (num_bodies < 0) return ogx_fail(OGX_ERR_INVALID, "num_bodies < 0");
+  std::vector<BodyRef> refs(num_bodies);
+  std::vector<int64_t> voff(num_bodies);
+  uint64_t quad = 0;
+  int64_t pts = 0;
+  for (int b = 0; b < num_bodies; ++b) {
+    if (counts[b] < 1) return ogx_fail(OGX_ERR_INVALID, "body %d has %d points", b, counts[b]);
+    refs[b].quad = (uint32_t)quad;
+    refs[b].n = counts[b];
+    voff[b] = pts;
+    quad += 3 * (uint64_t)((counts[b] + 3) / 4);
+    pts += counts[b];
+    if (quad >= (1ull << 32))
+      return ogx_fail(OGX_ERR_CAPACITY, "pool exceeds 2^32 float4 blocks (%.1f GB)", quad * 16e-9);
+  }
+  cudaSetDevice(ctx->device);
+  ogx_pool* p = new ogx_pool();
+  p->ctx = ctx;
+  p->nbodies = num_bodies;
+  p->npoints = pts;
+  p->nfloats = 4 * quad;
+  cudaError_t e;
+  if ((e = cudaMalloc(&p->d_points, std::max<size_t>(16, p->nfloats * sizeof(float)))) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_bodies, std::max<size_t>(8, num_bodies * sizeof(BodyRef)))) != cudaSuccess ||
+      (e = cudaMalloc(&p->d_voff, std::max<size_t>(8, num_bodies * sizeof(int64_t)))) != cudaSuccess) {
+    ogx_pool_destroy(p);
+    return ogx_cuda_fail(e, "pool allocation");
+  }
+  if (num_bodies > 0) {
+    if ((e = cudaMemcpy(p->d_bodies, refs.data(), num_bodies * sizeof(BodyRef),
+                        cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(p->d_voff, voff.data(), num_bodies * sizeof(int64_t),
+                        cudaMemcpyHostToDevice)) != cudaSuccess) {
+      ogx_pool_destroy(p);
+      return ogx_cuda_fail(e, "pool table upload");
+    }
+  }
+  *out = p;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_pool_destroy(ogx_pool* p) {
+  if (!p) return OGX_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  cudaFree(p->d_points);
+  cudaFree(p->d_bodies);
+  cudaFree(p->d_voff);
+  delete p;
+  return OGX_OK;
+}
+
+extern "C" int ogx_pool_num_bodies(const ogx_pool* p) { return p ? p->nbodies : 0; }
+extern "C" int64_t ogx_pool_num_points(const ogx_pool* p) { return p ? p->npoints : 0; }
+
+extern "C" ogx_status ogx_pool_device_layout(const ogx_pool* p, float** d_points, void** d_bodies) {
+  if (!p) return ogx_fail(OGX_ERR_INVALID, "pool is NULL");
+  if (d_points) *d_points = p->d_points;
+  if (d_bodies) *d_bodies = p->d_bodies;
+  return OGX_OK;
+}
+
+ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos) {
+  if (p->nbodies == 0) return OGX_OK;
+  cudaError_t e = launch_pack(d_aos, p->d_voff, p->d_bodies, p->nbodies, p->d_points, g_grid_pack,
+                              ctx->stream);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "k_pack launch");
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_pool_load_device(ogx_ctx* ctx, ogx_pool* p, const float* d_coords) {
+  if (!ctx || !p || (!d_coords && p->npoints > 0)) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  cudaSetDevice(ctx->device);
+  ctx->last_launches = 0;
+  ogx_status s = pool_pack(ctx, p, d_coords);
+  if (!s) ctx->last_launches = p->nbodies ? 1 : 0;
+  return s;
+}
+
+extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* coords) {
+  if (!ctx || !p || (!coords && p->npoints > 0)) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  if (p->npoints == 0) return OGX_OK;
+  cudaSetDevice(ctx->device);
+  const size_t bytes = (size_t)p->npoints * 3 * sizeof(float);
+  cudaPointerAttributes attr;
+  const bool pinned = cudaPointerGetAttributes(&attr, coords) == cudaSuccess &&
+                      (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
+  cudaGetLastError();
+  ogx_status s = ctx->ensure_stage(pinned ? 0 : bytes, bytes);
+  if (s) return s;
+  const void* src = coords;
+  if (!pinned) {
+    // stage pageable memory through the pinned buffer (parallel host copy)
+    cudaStreamSynchronize(ctx->stream);  // the pinned buffer may still be in use
+    const int nt = (int)std::min<size_t>(16, std::max<size_t>(1, bytes >> 24));
+    std::vector<std::thread> th;
+    for (int k = 0; k < nt; ++k)
+      th.emplace_back([&, k] {
+        const size_t lo = bytes * k / nt, hi = bytes * (k + 1) / nt;
+        memcpy((char*)ctx->h_stage + lo, (const char*)coords + lo, hi - lo);
+      });
+    for (auto& x : th) x.join();
+    src = ctx->h_stage;
+  }
+  cudaError_t e = cudaMemcpyAsync(ctx->d_stage, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "pool upload copy");
+  ctx->last_launches = 0;
+  s = pool_pack(ctx, p, static_cast<const float*>(ctx->d_stage));
+  if (!s) ctx->last_launches = 1;
+  return s;
+}
+
+// ---------------------------------------------------------------------------------
+// batched queries
+
+ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, int nbodies,
+                   int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
+                   float* d_nrm, int32_t* d_status, int mode) {
+  if (npairs < 0) return ogx_fail(OGX_ERR_INVALID, "npairs < 0");
+  if (npairs == 0) {
+    ctx->last_launches = 0;
+    return OGX_OK;
+  }
+  if (!d_pairs || !d_smp || !d_dist || (mode != kModeGjk && !d_nrm))
+    return ogx_fail(OGX_ERR_INVALID, "NULL output or pair buffer");
+  cudaSetDevice(ctx->device);
+  ogx_status s = ctx->ensure_scratch(npairs);
+  if (s) return s;
+  DevBatch B;
+  B.pool = d_pool;
+  B.bodies = d_bodies;
+  B.nbodies = nbodies;
+  B.pairs = reinterpret_cast<const int2*>(d_pairs);
+  B.npairs = npairs;
+  B.smp = d_smp;
+  B.dist = d_dist;
+  B.nrm = d_nrm;
+  B.status = d_status;
+  B.lists = ctx->d_lists;
+  B.elists = ctx->d_elists;
+  B.counts = ctx->d_counts;
+  B.polish = ctx->d_polish;
+  B.refine = ctx->d_refine;
+  B.cfg = ctx->cfg;
+  B.mode = mode;
+  cudaStream_t st = ctx->stream;
+  int launches = 0;
+  ctx->ev_count = 0;
+  static const char* kGjkName[kBuckets] = {"gjk<=16", "gjk<=32", "gjk<=64", "gjk<=128",
+                                           "gjk<=256", "gjk<=512", "gjk>512"};
+  static const char* kEpaName[kBuckets] = {"epa<=16", "epa<=32", "epa<=64", "epa<=128",
+                                           "epa<=256", "epa<=512", "epa>512"};
+  cudaError_t e = cudaMemsetAsync(ctx->d_counts, 0, kCntSlots * sizeof(int), st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "counter reset");
+  const int bin_grid = std::min(g_grid_bin, (npairs + 255) / 256);
+  ctx->mark("bin");
+  e = launch_bin(B, bin_grid, st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "k_bin launch");
+  ++launches;
+  if (mode != kModeEpa) {
+    for (int b = kBuckets - 1; b >= 0; --b) {
+      ctx->mark(kGjkName[b]);
+      g_gjk[b].fn<<<g_gjk[b].grid, kBlock, 0, st>>>(B, b);
+      ++launches;
+    }
+  }
+  if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
+    ctx->mark("refine");
+    e = launch_refine(B, g_grid_refine, st);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
+    ++launches;
+  }
+  if (mode != kModeGjk) {
+    for (int b = kBuckets - 1; b >= 0; --b) {
+      ctx->mark(kEpaName[b]);
+      g_epa[b].fn<<<g_epa[b].grid, kBlock, g_epa[b].smem, st>>>(B, b);
+      ++launches;
+    }
+  }
+  if (mode != kModeGjk && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
+    ctx->mark("polish");
+    e = launch_polish(B, g_grid_polish, st);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
+    ++launches;
+  }
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "pipeline launch");
+  if (ctx->timing) cudaEventRecord(ctx->ev[ctx->ev_count], st);
+  ctx->last_launches = launches;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_gjk(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                              const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                              float* d_distances, int32_t* d_status) {
+  if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
+  return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
+                 d_distances, nullptr, d_status, kModeGjk);
+}
+
+extern "C" ogx_status ogx_gjk_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                                  const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                                  float* d_distances, float* d_normals, int32_t* d_status) {
+  if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
+  return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
+                 d_distances, d_normals, d_status, kModeGjkEpa);
+}
+
+extern "C" ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                              const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                              float* d_distances, float* d_normals, int32_t* d_status) {
+  if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
+  return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
+                 d_distances, d_normals, d_status, kModeEpa);
+}

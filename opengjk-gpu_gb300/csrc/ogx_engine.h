@@ -1,0 +1,58 @@
+// ogx_engine.h -- internal declarations shared by the engine's .cu files.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdarg.h>
+
+#include "ogx.h"
+#include "ogx_kernels.cuh"
+
+struct ogx_ctx {
+  int device = 0;
+  int sm_count = 0;
+  ogx_config cfg;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // per-call work lists (grown on demand)
+  int* d_lists = nullptr;
+  int* d_elists = nullptr;
+  int* d_counts = nullptr;
+  ogx::PolishRec* d_polish = nullptr;
+  int* d_refine = nullptr;
+  size_t cap_pairs = 0;
+  // staging for host uploads
+  void* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
+  void* d_stage = nullptr;
+  size_t d_stage_bytes = 0;
+  int last_launches = 0;
+  // optional per-launch timing (CUDA events recorded between the launches of a call)
+  bool timing = false;
+  static constexpr int kMaxTimed = 32;
+  cudaEvent_t ev[kMaxTimed + 1] = {};
+  const char* ev_name[kMaxTimed] = {};
+  int ev_count = 0;
+
+  void mark(const char* name);  // record an event before the next launch
+
+  ogx_status ensure_scratch(int npairs);
+  ogx_status ensure_stage(size_t host_bytes, size_t dev_bytes);
+  void free_scratch();
+};
+
+struct ogx_pool {
+  ogx_ctx* ctx = nullptr;
+  int nbodies = 0;
+  int64_t npoints = 0;
+  size_t nfloats = 0;
+  float* d_points = nullptr;
+  ogx::BodyRef* d_bodies = nullptr;
+  int64_t* d_voff = nullptr;  // first point of each body in the AoS source
+};
+
+ogx_status ogx_fail(ogx_status s, const char* fmt, ...);
+ogx_status ogx_cuda_fail(cudaError_t e, const char* what);
+ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos);
+ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const ogx::BodyRef* d_bodies, int nbodies,
+                   int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
+                   float* d_nrm, int32_t* d_status, int mode);

@@ -443,7 +443,19 @@ struct GjkState {
   fv3 w0, w1;   // witnesses on body 1 and body 2
   int iters;
   int status;
+  int exit;     // why the loop ended (GJK_EXIT_*)
   bool polish;  // the FP32 distance is not known to polish_rel: re-solve in FP64
+};
+
+// loop exit reasons (reported in status bits 16..18)
+enum {
+  GJK_EXIT_GAP_REL = 1,   // |v|^2 - v.w <= eps_rel |v|^2
+  GJK_EXIT_GAP_NOISE = 2, // gap below the FP32 rounding floor (or eps_tot)
+  GJK_EXIT_NULL_V = 3,    // |v| < eps_rel
+  GJK_EXIT_DUPLICATE = 4, // support pair already in the simplex
+  GJK_EXIT_CONTACT = 5,   // |v| negligible against the simplex scale
+  GJK_EXIT_ENCLOSED = 6,  // origin inside the tetrahedron
+  GJK_EXIT_CAP = 7,       // iteration cap
 };
 
 // The pair is in contact (EPA runs) when GJK enclosed the origin or the distance is
@@ -499,11 +511,13 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
   g.ia[0] = 0;
   g.ib[0] = 0;
   g.status = 0;
+  g.exit = 0;
   g.wmax2 = 0.0f;
   fv3 sa = a0, sb = b0;
   int ia = 0, ib = 0;
   const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
-  const float contact = reftol ? cfg.gjk_eps_tot : cfg.gjk_noise * FLT_EPSILON;
+  // |v| this small against the simplex points is below FP32 resolution: stop
+  const float contact = reftol ? cfg.gjk_eps_tot : 0.5f * FLT_EPSILON;
   int k = 0;
   for (;;) {
     ++k;
@@ -530,12 +544,25 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
       const float nv = sqrtf(vv);
       floor_ = fmaxf(floor_, cfg.gjk_noise * FLT_EPSILON * nv * (nv + sqrtf(dot(w, w))));
     }
-    if (gap <= cfg.gjk_eps_rel * vv || gap < floor_) break;
-    if (vv < eps_rel2) break;
+    if (gap <= cfg.gjk_eps_rel * vv) {
+      g.exit = GJK_EXIT_GAP_REL;
+      break;
+    }
+    if (gap < floor_) {
+      g.exit = GJK_EXIT_GAP_NOISE;
+      break;
+    }
+    if (vv < eps_rel2) {
+      g.exit = GJK_EXIT_NULL_V;
+      break;
+    }
     if (!reftol) {
       bool dup = false;
       for (int j = 0; j < g.n; ++j) dup |= (g.ia[j] == ia && g.ib[j] == ib);
-      if (dup) break;
+      if (dup) {
+        g.exit = GJK_EXIT_DUPLICATE;
+        break;
+      }
     }
     g.P[g.n] = w;
     g.ia[g.n] = ia;
@@ -587,9 +614,20 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
       g.n = nn;
     }
     for (int j = 0; j < g.n; ++j) g.wmax2 = fmaxf(g.wmax2, dot(g.P[j], g.P[j]));
-    if (dot(v, v) <= contact * contact * g.wmax2) break;
-    if (g.n == 4 || k == cfg.gjk_max_iter) break;
+    if (dot(v, v) <= contact * contact * g.wmax2) {
+      g.exit = GJK_EXIT_CONTACT;
+      break;
+    }
+    if (g.n == 4) {
+      g.exit = GJK_EXIT_ENCLOSED;
+      break;
+    }
+    if (k == cfg.gjk_max_iter) {
+      g.exit = GJK_EXIT_CAP;
+      break;
+    }
   }
+  g.status |= g.exit << 16;
   if (k == cfg.gjk_max_iter && g.n != 4) g.status |= OGX_S_GJK_CAP;
   g.iters = k;
   g.v = v;
@@ -612,6 +650,178 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
     const float errb = 16.0f * FLT_EPSILON * sqrtf(g.wmax2);
     g.polish = errb > cfg.polish_rel * g.dist;
   }
+}
+
+// Exact (FP64) support index of body w along d.  An FP32 scan finds the maximum m of
+// fl(x . d32); every point whose exact value could exceed the true maximum satisfies
+// fl(x . d32) >= m - 2e with e >= |fl(x . d32) - x . d| <= 2 FLT_EPSILON |x|_max |d|_1
+// (rounding of d to FP32 plus the FP32 dot product), so only those few candidates are
+// evaluated in FP64.  Ties go to the lowest index.
+template <class Bodies>
+OGX_HD int exact_support(const Bodies& B, int w, dv3 d, double& val) {
+  const MemBodies& M = B.mem_view();
+  const fv3 fd = cvt<float>(d);
+  const float* X = M.base[w];
+  const float* Y = X + M.n4[w];
+  const float* Z = Y + M.n4[w];
+  const int n = M.n[w];
+  float m = -INFINITY, amax = 0.0f;
+  for (int i = 0; i < n; ++i) {
+    m = fmaxf(m, sdot(X[i], Y[i], Z[i], fd));
+    amax = fmaxf(amax, fmaxf(fabsf(X[i]), fmaxf(fabsf(Y[i]), fabsf(Z[i]))));
+  }
+  const float e = 4.0f * FLT_EPSILON * amax * (fabsf(fd.x) + fabsf(fd.y) + fabsf(fd.z)) + FLT_MIN;
+  const float lo = m - 2.0f * e;
+  double best = -INFINITY;
+  int bi = 0;
+  for (int i = 0; i < n; ++i) {
+    if (sdot(X[i], Y[i], Z[i], fd) < lo) continue;
+    const double x = (double)X[i] * d.x + (double)Y[i] * d.y + (double)Z[i] * d.z;
+    if (x > best) {
+      best = x;
+      bi = i;
+    }
+  }
+  val = best;
+  return bi;
+}
+
+// FP64 continuation of GJK from the FP32 result: exact supports, FP64 sub-distance,
+// stop when the FP64 gap |v|^2 - v.w <= 1e-13 |v|^2 or the support repeats.  Certifies
+// (or corrects) the FP32 answer; sets g.n = 4 if the origin turns out to be enclosed.
+template <class Bodies>
+OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
+  Sx<double> s;
+  int ia[4], ib[4];
+  s.n = g.n > 3 ? 3 : g.n;
+  for (int j = 0; j < s.n; ++j) {
+    ia[j] = g.ia[j];
+    ib[j] = g.ib[j];
+    s.v[j].p = B.dpoint(0, ia[j]) - B.dpoint(1, ib[j]);
+    s.v[j].k = j;
+  }
+  // exact closest point of the FP32 result's simplex; keep only the vertices it uses
+  dv3 P[3];
+  for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
+  double lam[4];
+  dv3 v;
+  closest_on_simplex(s.n, P, lam, v);
+  {
+    Sx<double> r;
+    r.n = 0;
+    int ra[4], rb[4];
+    for (int j = 0; j < s.n; ++j)
+      if (lam[j] > 0.0 || (s.n == 1)) {
+        r.v[r.n] = s.v[j];
+        ra[r.n] = ia[j];
+        rb[r.n] = ib[j];
+        r.n++;
+      }
+    if (r.n == 0) {
+      r.v[0] = s.v[0];
+      ra[0] = ia[0];
+      rb[0] = ib[0];
+      r.n = 1;
+    }
+    s = r;
+    for (int j = 0; j < s.n; ++j) {
+      ia[j] = ra[j];
+      ib[j] = rb[j];
+      s.v[j].k = j;
+    }
+  }
+  int it = 0;
+  bool enclosed = false;
+  double wmax2 = 0.0;
+  for (int j = 0; j < s.n; ++j) wmax2 = fmax(wmax2, dot(s.v[j].p, s.v[j].p));
+  for (; it < max_iter; ++it) {
+    double va, vb;
+    const int xa = exact_support(B, 0, -v, va);
+    const int xb = exact_support(B, 1, v, vb);
+    const dv3 w = B.dpoint(0, xa) - B.dpoint(1, xb);
+    const double vv = dot(v, v);
+    // FP64 gap test.  In exact arithmetic v.p_j = |v|^2 for every vertex p_j of the
+    // current feature, so the gap |v|^2 - v.w equals v.(p_j - w); that form rounds in
+    // proportion to |p_j - w| (small near convergence) instead of |w|^2.  Relative
+    // tolerance of the FP64 oracle (eps * 1e4) and a rounding floor.
+    double gap = INFINITY, dmax = 0.0;
+    for (int j = 0; j < s.n; ++j) {
+      const dv3 e = s.v[j].p - w;
+      gap = fmin(gap, dot(v, e));
+      dmax = fmax(dmax, dot(e, e));
+    }
+    const double floor64 = 64.0 * DBL_EPSILON * sqrt(wmax2) * sqrt(dmax);
+#ifdef OGX_TRACE
+    printf("refine it %d: n=%d |v|=%.12g support (%d,%d) gap %.3g floor %.3g\n", it, s.n, sqrt(vv), xa, xb, gap, floor64);
+#endif
+    if (gap <= 1e-12 * vv || gap <= floor64) break;
+    bool dup = false;
+    for (int j = 0; j < s.n; ++j) dup |= (ia[j] == xa && ib[j] == xb);
+    if (dup) break;
+    const Sx<double> prev = s;
+    int pa[4], pb[4];
+    for (int j = 0; j < s.n; ++j) {
+      pa[j] = ia[j];
+      pb[j] = ib[j];
+    }
+    const dv3 vprev = v;
+    s.v[s.n].p = w;
+    s.v[s.n].k = s.n;
+    ia[s.n] = xa;
+    ib[s.n] = xb;
+    s.n++;
+    Unc u{false};
+    subdistance(s, v, u);
+    if (s.n != 4 && !(dot(v, v) < vv * (1.0 - 1e-12))) {
+      // no progress: a tie support spanning a degenerate simplex -- keep the last answer
+      s = prev;
+      v = vprev;
+      for (int j = 0; j < s.n; ++j) {
+        ia[j] = pa[j];
+        ib[j] = pb[j];
+      }
+      break;
+    }
+    int na[4], nb[4];
+    for (int j = 0; j < s.n; ++j) {
+      na[j] = ia[s.v[j].k];
+      nb[j] = ib[s.v[j].k];
+    }
+    for (int j = 0; j < s.n; ++j) {
+      ia[j] = na[j];
+      ib[j] = nb[j];
+      s.v[j].k = j;
+      wmax2 = fmax(wmax2, dot(s.v[j].p, s.v[j].p));
+    }
+    if (s.n == 4) {
+      enclosed = true;
+      break;
+    }
+  }
+  g.n = s.n;
+  for (int j = 0; j < s.n; ++j) {
+    g.ia[j] = ia[j];
+    g.ib[j] = ib[j];
+    g.P[j] = cvt<float>(s.v[j].p);
+  }
+  g.status |= OGX_S_POLISHED;
+  if (it == max_iter) g.status |= OGX_S_GJK_CAP;
+  if (enclosed) {
+    g.v = v3<float>(0.f, 0.f, 0.f);
+    g.dist = 0.0f;
+    return;
+  }
+  for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
+  closest_on_simplex(s.n, P, lam, v);
+  dv3 w0 = v3<double>(0.0, 0.0, 0.0), w1 = w0;
+  for (int j = 0; j < s.n; ++j) {
+    w0 = w0 + B.dpoint(0, ia[j]) * lam[j];
+    w1 = w1 + B.dpoint(1, ib[j]) * lam[j];
+  }
+  g.v = cvt<float>(v);
+  g.dist = (float)sqrt(dot(v, v));
+  g.w0 = cvt<float>(w0);
+  g.w1 = cvt<float>(w1);
 }
 
 // FP64 re-solve of the final simplex: exact Minkowski points, exact closest point.

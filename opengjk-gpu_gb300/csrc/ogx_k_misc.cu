@@ -1,0 +1,181 @@
+// ogx_k_misc.cu -- pool packing, pair binning and the FP64 polish pass.
+#include "ogx_kernels.cuh"
+
+namespace ogx {
+
+// ---------------------------------------------------------------------------------
+__global__ void k_pack(const float* __restrict__ aos, const int64_t* __restrict__ voff,
+                       const BodyRef* __restrict__ bodies, int nbodies, float* __restrict__ pool) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int b = warp; b < nbodies; b += nwarps) {
+    const BodyRef r = bodies[b];
+    const int n4 = round4(r.n);
+    const float* src = aos + 3 * voff[b];
+    float* dst = pool + 4 * (size_t)r.quad;
+    for (int i = lane; i < n4; i += 32) {
+      const int s = i < r.n ? i : 0;
+      dst[i] = src[3 * s];
+      dst[n4 + i] = src[3 * s + 1];
+      dst[2 * n4 + i] = src[3 * s + 2];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ bool pair_ok(const DevBatch& B, int2 pr) {
+  return pr.x >= 0 && pr.x < B.nbodies && pr.y >= 0 && pr.y < B.nbodies;
+}
+
+__device__ __forceinline__ void mark_bad(const DevBatch& B, int p) {
+  B.dist[p] = __int_as_float(0x7fc00000);
+  if (B.status) B.status[p] = OGX_S_BAD_INPUT;
+  if (B.nrm) store3(B.nrm + 3 * (size_t)p, v3<float>(1.f, 0.f, 0.f));
+  if (B.mode != kModeEpa) B.smp[p].nvrtx = 0;
+}
+
+__global__ void k_bin(DevBatch B) {
+  const int stride = gridDim.x * blockDim.x;
+  const int n32 = (B.npairs + 31) & ~31;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n32; p += stride) {
+    const bool in = p < B.npairs;
+    int b = -1;
+    bool bad = false;
+    bool work = false;
+    if (in) {
+      const int2 pr = B.pairs[p];
+      bad = !pair_ok(B, pr);
+      if (!bad) {
+        const int na = B.bodies[pr.x].n, nb = B.bodies[pr.y].n;
+        bad = na < 1 || nb < 1;
+        b = bucket_of(na > nb ? na : nb);
+      }
+      if (bad) {
+        mark_bad(B, p);
+      } else if (B.mode == kModeEpa) {
+        // EPA only: contacts go to the EPA lists, separated pairs only get a normal
+        const gkSimplex& s = B.smp[p];
+        work = s.nvrtx == 4 || !(B.dist[p] > FLT_EPSILON);
+        if (!work) {
+          const fv3 w0 = v3<float>(s.witnesses[0][0], s.witnesses[0][1], s.witnesses[0][2]);
+          const fv3 w1 = v3<float>(s.witnesses[1][0], s.witnesses[1][1], s.witnesses[1][2]);
+          store3(B.nrm + 3 * (size_t)p, unit_or_x(w1 - w0));
+          if (B.status) B.status[p] = 0;
+        }
+      } else {
+        work = true;
+      }
+    }
+    // warp-aggregated append per bucket
+    const int key = work ? b : -1;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int wl = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    if (key >= 0) {
+      int* ctr = B.counts + (B.mode == kModeEpa ? kCntEpa : kCntGjk) + key;
+      int* list = (B.mode == kModeEpa ? B.elists : B.lists) + (size_t)key * B.npairs;
+      int base = 0;
+      if (wl == leader) base = atomicAdd(ctr, __popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      list[base + __popc(peers & ((1u << wl) - 1u))] = p;
+    }
+  }
+}
+
+// FP64 continuation of GJK for the pairs whose FP32 distance is not certain (one thread
+// per pair: the FP64 units see full warps).  A pair found enclosed joins its bucket's
+// EPA list; the others get their normal from the refined witnesses.
+__global__ void __launch_bounds__(128) k_refine(DevBatch B) {
+  const int cnt = B.counts[kCntRefine];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const int p = B.refine[k];
+    const int2 pr = B.pairs[p];
+    const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
+    MemBodies mb;
+    mb.bind(B.pool, ra, rb);
+    gkSimplex* s = B.smp + p;
+    GjkState g;
+    load_simplex(s, B.dist[p], g);
+    gjk_refine(mb, g, kRefineIters);
+    store_simplex(s, g);
+    B.dist[p] = g.dist;
+    if (B.status) B.status[p] |= g.status;
+    const bool contact = gjk_contact(g);
+    if (B.mode == kModeGjkEpa) {
+      if (contact) {
+        const int bucket = bucket_of(ra.n > rb.n ? ra.n : rb.n);
+        const int e = atomicAdd(B.counts + kCntEpa + bucket, 1);
+        B.elists[(size_t)bucket * B.npairs + e] = p;
+      } else {
+        store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) k_polish(DevBatch B) {
+  const int cnt = B.counts[kCntPolish];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
+    const PolishRec r = B.polish[k];
+    const int p = r.pair;
+    const int2 pr = B.pairs[p];
+    MemBodies mb;
+    mb.bind(B.pool, B.bodies[pr.x], B.bodies[pr.y]);
+    gkSimplex* s = B.smp + p;
+    {
+      EpaOut o;
+      for (int m = 0; m < 3; ++m) {
+        o.face[m][0] = r.face[m][0];
+        o.face[m][1] = r.face[m][1];
+      }
+      const float* n = B.nrm + 3 * (size_t)p;
+      o.nrm = v3<float>(n[0], n[1], n[2]);
+      o.dist = B.dist[p];
+      o.status = 0;
+      epa_polish(mb, o);
+      if (!(o.status & OGX_S_POLISHED)) continue;
+      B.dist[p] = o.dist;
+      s->witnesses[0][0] = o.w0.x;
+      s->witnesses[0][1] = o.w0.y;
+      s->witnesses[0][2] = o.w0.z;
+      s->witnesses[1][0] = o.w1.x;
+      s->witnesses[1][1] = o.w1.y;
+      s->witnesses[1][2] = o.w1.z;
+      store3(B.nrm + 3 * (size_t)p, o.nrm);
+    }
+    if (B.status) B.status[p] |= OGX_S_POLISHED;
+  }
+}
+
+
+cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
+                        float* pool, int grid, cudaStream_t st) {
+  k_pack<<<grid, 256, 0, st>>>(aos, voff, bodies, nbodies, pool);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
+  k_bin<<<grid, 256, 0, st>>>(B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
+  k_polish<<<grid, 128, 0, st>>>(B);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_refine(const DevBatch& B, int grid, cudaStream_t st) {
+  k_refine<<<grid, 128, 0, st>>>(B);
+  return cudaGetLastError();
+}
+
+cudaError_t refine_occupancy(int block, int* per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_refine, block, 0);
+}
+
+cudaError_t polish_occupancy(int block, int* per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_polish, block, 0);
+}
+
+}  // namespace ogx

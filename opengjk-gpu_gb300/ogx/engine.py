@@ -1,0 +1,203 @@
+"""Python host side of the engine API: contexts, device pools and batched queries.
+
+Device buffers are torch CUDA tensors (torch is only the allocator and stream
+provider here); every computation is a call into libogx.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import SIMPLEX_DTYPE, check
+
+MODE_GJK, MODE_GJK_EPA, MODE_EPA = 1, 2, 3
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Context:
+    """One engine instance on one GPU, bound to a CUDA stream (default: torch's
+    current stream, so that engine calls order with torch work)."""
+
+    def __init__(self, device: int = 0, config: _lib.Config | None = None, stream=None):
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise _lib.OgxError(-4, "no CUDA device visible")
+        self.lib = _lib.load()
+        self.device = device
+        torch.cuda.set_device(device)
+        if stream is None:
+            stream = torch.cuda.current_stream(device)
+        self.stream = stream
+        h = ctypes.c_void_p()
+        cfgp = ctypes.byref(config) if config is not None else None
+        check(self.lib.ogx_ctx_create(device, cfgp, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.ogx_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def config(self) -> _lib.Config:
+        c = _lib.Config()
+        check(self.lib.ogx_ctx_get_config(self.handle, ctypes.byref(c)))
+        return c
+
+    @config.setter
+    def config(self, c: _lib.Config):
+        check(self.lib.ogx_ctx_set_config(self.handle, ctypes.byref(c)))
+
+    def set_stream(self, stream):
+        self.stream = stream
+        check(self.lib.ogx_ctx_set_stream(self.handle, ctypes.c_void_p(stream.cuda_stream)))
+
+    def synchronize(self):
+        check(self.lib.ogx_ctx_synchronize(self.handle))
+
+    @property
+    def last_launches(self) -> int:
+        return int(self.lib.ogx_ctx_last_launches(self.handle))
+
+    def set_timing(self, on: bool = True):
+        check(self.lib.ogx_ctx_set_timing(self.handle, int(on)))
+
+    def kernel_times(self) -> list:
+        """[(kernel name, ms)] of the last batched call (needs set_timing(True))."""
+        names = (ctypes.c_char_p * 32)()
+        ms = (ctypes.c_float * 32)()
+        n = self.lib.ogx_ctx_kernel_times(self.handle, names, ms, 32)
+        if n < 0:
+            raise _lib.OgxError(-2, "kernel timing failed")
+        return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+    def work_counts(self) -> dict:
+        c = (ctypes.c_int32 * 16)()
+        n = self.lib.ogx_ctx_work_counts(self.handle, c, 16)
+        if n != 16:
+            raise _lib.OgxError(-2, "work counts unavailable")
+        return {"gjk": list(c[0:7]), "epa": list(c[7:14]), "polish": int(c[14]), "refine": int(c[15])}
+
+
+class Pool:
+    """Device-resident polytope pool (padded SoA layout)."""
+
+    def __init__(self, ctx: Context, counts):
+        self.ctx = ctx
+        counts = np.ascontiguousarray(counts, dtype=np.int32)
+        self.counts = counts
+        h = ctypes.c_void_p()
+        check(ctx.lib.ogx_pool_create(ctx.handle, int(counts.shape[0]), counts.ctypes.data, ctypes.byref(h)))
+        self.handle = h
+
+    @property
+    def num_bodies(self) -> int:
+        return int(self.ctx.lib.ogx_pool_num_bodies(self.handle))
+
+    @property
+    def num_points(self) -> int:
+        return int(self.ctx.lib.ogx_pool_num_points(self.handle))
+
+    def upload(self, coords):
+        """coords: host (numpy, or pinned torch CPU tensor) float32 xyz of all bodies."""
+        torch = _torch()
+        if isinstance(coords, torch.Tensor):
+            assert coords.device.type == "cpu" and coords.dtype == torch.float32 and coords.is_contiguous()
+            ptr = coords.data_ptr()
+            self._keep = coords
+        else:
+            arr = np.ascontiguousarray(coords, dtype=np.float32)
+            ptr = arr.ctypes.data
+            self._keep = arr
+        check(self.ctx.lib.ogx_pool_upload(self.ctx.handle, self.handle, ctypes.c_void_p(ptr)))
+
+    def load_device(self, coords_dev):
+        """coords_dev: torch CUDA float32 tensor, xyz of all bodies (AoS)."""
+        assert coords_dev.is_cuda and coords_dev.dtype == _torch().float32 and coords_dev.is_contiguous()
+        check(self.ctx.lib.ogx_pool_load_device(self.ctx.handle, self.handle, ctypes.c_void_p(coords_dev.data_ptr())))
+
+    def device_layout(self):
+        pts, bodies = ctypes.c_void_p(), ctypes.c_void_p()
+        check(self.ctx.lib.ogx_pool_device_layout(self.handle, ctypes.byref(pts), ctypes.byref(bodies)))
+        return pts.value, bodies.value
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.ogx_pool_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Results:
+    """Device outputs of one batched call (torch CUDA tensors)."""
+
+    def __init__(self, n: int, device, with_normals: bool = True):
+        torch = _torch()
+        self.n = n
+        self.simplex = torch.zeros((n, 27), dtype=torch.int32, device=device)  # 108 B per pair
+        self.dist = torch.zeros(n, dtype=torch.float32, device=device)
+        self.normal = torch.zeros((n, 3), dtype=torch.float32, device=device) if with_normals else None
+        self.status = torch.zeros(n, dtype=torch.int32, device=device)
+
+    def to_host(self) -> dict:
+        smp = self.simplex.cpu().numpy().view(SIMPLEX_DTYPE).reshape(self.n)
+        out = {
+            "dist": self.dist.cpu().numpy(),
+            "simplex": smp,
+            "status": self.status.cpu().numpy(),
+        }
+        out["normal"] = self.normal.cpu().numpy() if self.normal is not None else None
+        return out
+
+
+def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Results | None = None) -> Results:
+    """Batched query over device pairs (int32 [n, 2] CUDA tensor)."""
+    torch = _torch()
+    assert pairs_dev.is_cuda and pairs_dev.dtype == torch.int32 and pairs_dev.is_contiguous()
+    n = int(pairs_dev.shape[0])
+    if out is None:
+        out = Results(n, pairs_dev.device, with_normals=(mode != MODE_GJK))
+    P = ctypes.c_void_p
+    args = [ctx.handle, pool.handle, n, P(pairs_dev.data_ptr()), P(out.simplex.data_ptr()), P(out.dist.data_ptr())]
+    if mode == MODE_GJK:
+        check(ctx.lib.ogx_gjk(*args, P(out.status.data_ptr())))
+    elif mode == MODE_GJK_EPA:
+        check(ctx.lib.ogx_gjk_epa(*args, P(out.normal.data_ptr()), P(out.status.data_ptr())))
+    elif mode == MODE_EPA:
+        check(ctx.lib.ogx_epa(*args, P(out.normal.data_ptr()), P(out.status.data_ptr())))
+    else:
+        raise ValueError(mode)
+    return out
+
+
+def query(batch, mode: int = MODE_GJK_EPA, config: _lib.Config | None = None, device: int = 0) -> dict:
+    """One-shot convenience: upload a workloads.Batch, run, return host numpy results."""
+    torch = _torch()
+    ctx = Context(device, config)
+    pool = Pool(ctx, batch.counts)
+    pool.upload(batch.coords)
+    pairs = torch.from_numpy(np.ascontiguousarray(batch.pairs, dtype=np.int32)).to(f"cuda:{device}")
+    res = run(ctx, pool, pairs, mode)
+    ctx.synchronize()
+    out = res.to_host()
+    out["launches"] = ctx.last_launches
+    pool.close()
+    ctx.close()
+    return out

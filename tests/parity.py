@@ -1,0 +1,155 @@
+"""Parity rules of the engine against the FP64 oracle (the reference's CPU GJK/EPA run
+in double precision on the same FP32 inputs widened exactly to double).
+
+Tolerances (stated once, used by every parity test):
+  * contact band: a pair whose oracle distance satisfies |d| <= BAND * s, with
+    s = max(1, largest |coordinate| of the pair), is "in the band" -- FP32 inputs cannot
+    decide its verdict; there only |d - d_oracle| <= 2 * BAND * s is required.
+  * verdict (contact / separated) identical outside the band.
+  * separated pairs outside the band: |d - d_oracle| <= REL * d_oracle (REL = 1e-5).
+  * contacts outside the band: |depth - depth_oracle| <= ABS4, normal within ABS4 (L2)
+    -- or, where the minimum-translation direction is ill-conditioned (dense point
+    clouds: many near-optimal faces), a normal along which the bodies' exact support
+    depth exceeds the oracle's depth by at most EQUIV * max(1, depth) (EQUIV = 1e-6);
+    witnesses satisfy w0 - w1 = depth * n and lie on the support planes of their bodies
+    within ABS4; where the oracle's own witnesses are self-consistent and the contact
+    features are unique, they agree with the oracle's within ABS4 (ABS4 = 1e-4).
+"""
+import numpy as np
+
+BAND = 1e-5
+REL = 1e-5
+ABS4 = 1e-4
+EQUIV = 1e-6
+
+
+def pair_scale(b):
+    m = np.maximum.reduceat(np.abs(b.coords).max(axis=1), b.offsets)
+    return np.maximum(1.0, np.maximum(m[b.pairs[:, 0]], m[b.pairs[:, 1]]))
+
+
+def support_gaps(b, w0, w1, n):
+    """n.w0 - max_A n.a  and  min_B n.b - n.w1 per pair (both ~0 for valid witnesses)."""
+    ga = np.empty(len(n))
+    gb = np.empty(len(n))
+    for i in range(len(n)):
+        A = b.body(b.pairs[i, 0]).astype(np.float64)
+        B = b.body(b.pairs[i, 1]).astype(np.float64)
+        ga[i] = n[i] @ w0[i] - (A @ n[i]).max()
+        gb[i] = (B @ n[i]).min() - n[i] @ w1[i]
+    return ga, gb
+
+
+def unique_contact(b, n, tol=1e-6):
+    """Contact features unique: at most 4 support points within tol of the planes."""
+    u = np.zeros(len(n), bool)
+    for i in range(len(n)):
+        A = b.body(b.pairs[i, 0]).astype(np.float64)
+        B = b.body(b.pairs[i, 1]).astype(np.float64)
+        pa, pb = A @ n[i], B @ n[i]
+        ca = np.sum(pa >= pa.max() - tol)
+        cb = np.sum(pb <= pb.min() + tol)
+        u[i] = (ca + cb <= 4) and not (ca >= 3 and cb >= 2) and not (cb >= 3 and ca >= 2)
+    return u
+
+
+def check(b, res, o, *, label="", witness_sample=2000, contact_status_bit=8):
+    """Compare engine results `res` (dict: dist, simplex, normal, status) with oracle
+    results `o` (orc.RESULT_DTYPE, FP64, GJK+EPA).  Returns a report; raises nothing."""
+    d = res["dist"].astype(np.float64)
+    d64 = o["dist"]
+    s = pair_scale(b)
+    band = np.abs(d64) <= BAND * s
+    col64 = o["epa_exit"] > 0
+    col = (res["status"] & contact_status_bit) != 0
+    rep = {"label": label, "pairs": len(d), "in_band": int(band.sum())}
+    rep["verdict_mismatch"] = int(np.sum((col != col64) & ~band))
+    rep["band_abs_violations"] = int(np.sum(band & (np.abs(d - d64) > 2 * BAND * s)))
+    sep = ~col64 & ~col & ~band
+    rel = np.abs(d[sep] - d64[sep]) / d64[sep] if sep.any() else np.zeros(0)
+    rep["separated"] = int(sep.sum())
+    rep["sep_rel_max"] = float(rel.max()) if rel.size else 0.0
+    rep["sep_rel_violations"] = int(np.sum(rel > REL))
+    both = col & col64 & ~band
+    rep["contacts"] = int(both.sum())
+    dd = np.abs(d[both] - d64[both])
+    rep["depth_err_max"] = float(dd.max()) if dd.size else 0.0
+    # A depth smaller than the oracle's is a certified improvement when the bodies'
+    # exact support depth along the engine's normal confirms it: any direction bounds
+    # the minimum translation distance from above (the reference EPA can stop on a
+    # wrong face when the origin lies almost on the Minkowski boundary).
+    bad = np.flatnonzero(both)[dd > ABS4]
+    better = 0
+    for i in bad:
+        if -d[i] < -d64[i]:
+            A = b.body(b.pairs[i, 0]).astype(np.float64)
+            B = b.body(b.pairs[i, 1]).astype(np.float64)
+            n = res["normal"][i].astype(np.float64)
+            n /= np.linalg.norm(n)
+            if (A @ n).max() - (B @ n).min() <= -d[i] + EQUIV * max(1.0, -d[i]):
+                better += 1
+    rep["oracle_suboptimal"] = better
+    rep["depth_violations"] = int(bad.size - better)
+    nn = np.linalg.norm(res["normal"][both].astype(np.float64) - o["normal"][both], axis=1)
+    rep["normal_err_max"] = float(nn.max()) if nn.size else 0.0
+    far = np.flatnonzero(both)[nn > ABS4]
+    equiv = 0
+    for i in far:
+        A = b.body(b.pairs[i, 0]).astype(np.float64)
+        B = b.body(b.pairs[i, 1]).astype(np.float64)
+        n = res["normal"][i].astype(np.float64)
+        n /= np.linalg.norm(n)
+        if (A @ n).max() - (B @ n).min() - (-d64[i]) <= EQUIV * max(1.0, -d64[i]):
+            equiv += 1
+    rep["normal_equivalent"] = equiv
+    rep["normal_violations"] = int(far.size - equiv)
+    # witnesses of contacts
+    idx = np.flatnonzero(both)[:witness_sample]
+    if idx.size:
+        w = res["simplex"]["witnesses"][idx].astype(np.float64)
+        n = res["normal"][idx].astype(np.float64)
+        depth = -d[idx]
+        incons = np.linalg.norm((w[:, 0] - w[:, 1]) - depth[:, None] * n, axis=1)
+        sb = b.subset(idx)
+        ga, gb = support_gaps(sb, w[:, 0], w[:, 1], n)
+        rep["witness_inconsistent"] = int(np.sum(incons > ABS4))
+        rep["witness_off_support"] = int(np.sum((np.abs(ga) > ABS4) | (np.abs(gb) > ABS4)))
+        ow = o["wit"][idx]
+        oincons = np.linalg.norm((ow[:, 0] - ow[:, 1]) - (-d64[idx])[:, None] * o["normal"][idx], axis=1)
+        ok = (oincons <= ABS4) & unique_contact(sb, o["normal"][idx])
+        werr = np.abs(w - ow).reshape(len(idx), -1).max(axis=1)
+        rep["witness_compared"] = int(ok.sum())
+        rep["witness_mismatch"] = int(np.sum(ok & (werr > ABS4)))
+    else:
+        rep.update(witness_inconsistent=0, witness_off_support=0, witness_compared=0, witness_mismatch=0)
+    # separated witnesses: w1 - w0 has length d; compared with the oracle's where the
+    # closest features are unique
+    sidx = np.flatnonzero(sep)[:witness_sample]
+    if sidx.size:
+        ws = res["simplex"]["witnesses"][sidx].astype(np.float64)
+        ow = o["wit"][sidx]
+        gap = np.abs(np.linalg.norm(ws[:, 1] - ws[:, 0], axis=1) - d64[sidx])
+        rep["sep_witness_length_violations"] = int(np.sum(gap > ABS4 * np.maximum(1.0, d64[sidx])))
+        dirn = ow[:, 1] - ow[:, 0]
+        dirn /= np.maximum(np.linalg.norm(dirn, axis=1, keepdims=True), 1e-300)
+        ok = unique_contact(b.subset(sidx), -dirn)
+        werr = np.abs(ws - ow).reshape(len(sidx), -1).max(axis=1)
+        rep["sep_witness_compared"] = int(ok.sum())
+        rep["sep_witness_err_max"] = float(werr[ok].max()) if ok.any() else 0.0
+        rep["sep_witness_violations"] = int(np.sum(ok & (werr > ABS4)))
+    return rep
+
+
+def assert_parity(rep, *, max_witness_mismatch_frac=1e-3, max_sep_witness_frac=1e-3):
+    msg = str(rep)
+    assert rep["verdict_mismatch"] == 0, msg
+    assert rep["band_abs_violations"] == 0, msg
+    assert rep["sep_rel_violations"] == 0, msg
+    assert rep["depth_violations"] == 0, msg
+    assert rep["normal_violations"] == 0, msg
+    assert rep["witness_inconsistent"] == 0, msg
+    assert rep["witness_off_support"] == 0, msg
+    assert rep["witness_mismatch"] <= max(1, max_witness_mismatch_frac * rep["witness_compared"]), msg
+    if "sep_witness_violations" in rep:
+        assert rep["sep_witness_length_violations"] == 0, msg
+        assert rep["sep_witness_violations"] <= max(1, max_sep_witness_frac * rep["sep_witness_compared"]), msg

@@ -1,0 +1,126 @@
+"""Edge cases of the GPU engine: empty batches, invalid indices, degenerate bodies,
+large bodies (memory-streamed bucket), determinism, mode consistency."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from ogx import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def test_empty_batch(engine):
+    import torch
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, np.array([4, 4], np.int32))
+    pool.upload(np.zeros((8, 3), np.float32))
+    pairs = torch.zeros((0, 2), dtype=torch.int32, device="cuda")
+    res = engine.run(ctx, pool, pairs)
+    ctx.synchronize()
+    assert res.dist.numel() == 0
+    assert ctx.last_launches == 0
+
+
+def test_bad_indices_flagged(engine):
+    import torch
+    from ogx import _lib
+    ctx = engine.Context(0)
+    b = W.plain(seed=3, n_pairs=4)
+    pool = engine.Pool(ctx, b.counts)
+    pool.upload(b.coords)
+    pairs = torch.tensor([[0, 1], [0, 99], [-1, 2], [2, 3]], dtype=torch.int32, device="cuda")
+    out = engine.run(ctx, pool, pairs).to_host()
+    st = out["status"]
+    assert st[1] & _lib.PAIR_BAD_INPUT and st[2] & _lib.PAIR_BAD_INPUT
+    assert np.isnan(out["dist"][1]) and np.isnan(out["dist"][2])
+    assert not (st[0] & _lib.PAIR_BAD_INPUT) and np.isfinite(out["dist"][[0, 3]]).all()
+
+
+def test_invalid_arguments_raise(engine):
+    from ogx import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    assert lib.ogx_ctx_create(0, None, None, ctypes.byref(h)) == 0
+    try:
+        pool = ctypes.c_void_p()
+        bad = np.array([3, 0], np.int32)
+        rc = lib.ogx_pool_create(h, 2, bad.ctypes.data, ctypes.byref(pool))
+        assert rc == -1 and b"points" in lib.ogx_last_error()
+        cfg = _lib.default_config()
+        cfg.epa_max_iter = 1000
+        assert lib.ogx_ctx_set_config(h, ctypes.byref(cfg)) == -1
+        assert lib.ogx_gjk(h, None, 1, None, None, None, None) == -1
+    finally:
+        lib.ogx_ctx_destroy(h)
+
+
+def test_degenerate_bodies(engine, orc):
+    """Single points, segments, identical and touching bodies follow the reference's
+    semantics (e.g. identical bodies: GJK starts at v = 0, EPA's simplex growth finds
+    no new point and reports depth 0, GJK/cpu/EPA.c:378-419)."""
+    rng = np.random.default_rng(5)
+    bodies = [
+        np.array([[0, 0, 0]], np.float32), np.array([[3, 0, 0]], np.float32),      # point-point
+        np.array([[0, 0, 0], [1, 0, 0]], np.float32), np.array([[0.5, 2, 0]], np.float32),  # segment-point
+        W.cube(), W.cube(),                                                          # identical cubes
+        W.cube(), (W.cube() + np.float32([2.0, 0, 0])),                              # touching faces
+        W.cube(), (W.cube() + np.float32([0.5, 0.3, 0.1])),                          # overlapping cubes
+        rng.normal(size=(7, 3)).astype(np.float32), np.array([[0.0, 0.0, 0.0]], np.float32),
+    ]
+    b = W.from_bodies(bodies)
+    res = engine.query(b, engine.MODE_GJK_EPA)
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64")
+    assert abs(res["dist"][0] - 3.0) < 1e-6
+    assert np.all(np.abs(res["dist"] - o["dist"]) < 1e-5), (res["dist"], o["dist"])
+    assert abs(res["dist"][4] + 1.5) < 1e-5  # overlapping cubes: depth 1.5 along x
+    assert np.all(np.isfinite(res["dist"]))
+    assert np.all(np.abs(np.linalg.norm(res["normal"], axis=1) - 1) < 1e-5)
+
+
+def test_large_bodies_streamed_bucket(engine, orc):
+    """Bodies above 512 points run from memory instead of registers."""
+    import parity
+    b = W.ellipsoid(seed=8, n_pairs=300, lo=600, hi=3000)
+    res = engine.query(b, engine.MODE_GJK_EPA)
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=16)
+    parity.assert_parity(parity.check(b, res, o, label="large"))
+
+
+def test_deterministic_and_batch_independent(engine):
+    """Each pair's result is the same alone and inside a larger mixed batch."""
+    b = W.powerlaw(seed=9, n_pairs=4000)
+    full = engine.query(b, engine.MODE_GJK_EPA)
+    again = engine.query(b, engine.MODE_GJK_EPA)
+    for k in ("dist", "normal", "status"):
+        assert np.array_equal(full[k], again[k])
+    sub = np.arange(0, 4000, 37)
+    part = engine.query(b.subset(sub), engine.MODE_GJK_EPA)
+    assert np.array_equal(part["dist"], full["dist"][sub])
+    assert np.array_equal(part["normal"], full["normal"][sub])
+
+
+def test_epa_only_matches_fused(engine):
+    import torch
+    b = W.ellipsoid(seed=10, n_pairs=2000)
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    pool.upload(b.coords)
+    pairs = torch.from_numpy(b.pairs).cuda()
+    fused = engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA).to_host()
+    r = engine.run(ctx, pool, pairs, engine.MODE_GJK)
+    engine.run(ctx, pool, pairs, engine.MODE_EPA, out=r)
+    sep = r.to_host()
+    assert np.array_equal(fused["dist"], sep["dist"])
+    assert np.allclose(fused["normal"], sep["normal"], atol=1e-6)
+
+
+def test_reference_tolerance_mode(engine, orc):
+    """With the reference's FP32 constants the engine stays within the reference's own
+    CPU-vs-GPU tolerance (1e-3, examples/main.cpp:184-188) of its FP32 CPU result."""
+    from ogx import _lib
+    b = W.ellipsoid(seed=12, n_pairs=5000)
+    res = engine.query(b, engine.MODE_GJK_EPA, config=_lib.reference_config())
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f32")
+    diff = np.abs(res["dist"] - o["dist"])
+    assert np.mean(diff <= 1e-3) > 0.995, np.mean(diff <= 1e-3)

@@ -1,0 +1,65 @@
+"""GPU engine (through the C ABI) against the FP64 oracle and the host build of the
+same per-pair code.  Tolerances: tests/parity.py."""
+import numpy as np
+import pytest
+
+import parity
+from ogx import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = ["set_plain", "set_ellipsoid", "set_powerlaw"]
+
+
+def _golden(name):
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{name}.npz"))
+    b = W.Batch(z["coords"], z["offsets"], z["counts"], z["pairs"], name)
+    o = np.zeros(b.n_pairs, dtype=__import__("oracle.orc", fromlist=["x"]).RESULT_DTYPE)
+    for f in o.dtype.names:
+        o[f] = z[f"f64_{f}"]
+    return b, o
+
+
+@pytest.mark.parametrize("name", GOLDEN)
+def test_golden_sets(engine, name):
+    b, o = _golden(name)
+    res = engine.query(b, engine.MODE_GJK_EPA)
+    rep = parity.check(b, res, o, label=name)
+    parity.assert_parity(rep)
+
+
+@pytest.mark.parametrize("gen,n", [(W.plain, 1000), (W.ellipsoid, 20000), (W.powerlaw, 20000)],
+                         ids=["plain_1k_fp64cfg", "ellipsoid_20k", "powerlaw_20k"])
+def test_workloads_vs_oracle(engine, orc, gen, n):
+    b = gen(n_pairs=n)
+    res = engine.query(b, engine.MODE_GJK_EPA)
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=16)
+    rep = parity.check(b, res, o, label=b.name)
+    print(rep)
+    parity.assert_parity(rep, max_witness_mismatch_frac=2e-3)
+
+
+def test_gpu_matches_host_build(engine, twin):
+    """Same per-pair code on the GPU (teams of 4-32 lanes) and on the CPU (one lane):
+    identical arithmetic, so results agree to the last bit except for rare ties."""
+    b = W.powerlaw(seed=21, n_pairs=5000)
+    g = engine.query(b, engine.MODE_GJK_EPA)
+    h = twin.run(b)
+    same_d = g["dist"] == h["dist"]
+    assert same_d.mean() > 0.995, same_d.mean()
+    close = np.abs(g["dist"].astype(np.float64) - h["dist"]) <= 1e-6 * np.maximum(1, np.abs(h["dist"]))
+    assert close.mean() > 0.999
+
+
+def test_gjk_only_mode(engine, orc):
+    b = W.ellipsoid(seed=22, n_pairs=3000)
+    res = engine.query(b, engine.MODE_GJK)
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK, precision="f64")
+    sep = (o["nvrtx"] < 4) & (o["dist"] > 1e-4)
+    d = res["dist"].astype(np.float64)
+    rel = np.abs(d[sep] - o["dist"][sep]) / o["dist"][sep]
+    assert rel.max() <= parity.REL
+    enclosed = o["nvrtx"] == 4
+    assert np.all(res["simplex"]["nvrtx"][enclosed] == 4)
+    assert np.all(d[enclosed] == 0.0)

@@ -40,8 +40,11 @@ void one(const Job& J, int i, EpaMem& M) {
   gjk_pair(t, B, *J.cfg, g);
   // same order as the device pipeline: the contact decision is taken on the FP32 GJK
   // result, separated pairs are then re-solved in FP64, contacts go through EPA
-  const bool contact = gjk_contact(g);
-  if (g.polish) gjk_polish(B, g);
+  bool contact = gjk_contact(g);
+  if (g.polish) {
+    gjk_refine(B, g, 16);
+    contact = gjk_contact(g);
+  }
   gkSimplex& s = J.smp[i];
   s.nvrtx = g.n;
   for (int k = 0; k < 4; ++k) {
