@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--pairs", type=int, default=0, help="override the workload's pair count")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the kernel autotuner")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
     return ap.parse_args()
@@ -213,6 +214,8 @@ def run_ours(args):
     pairs = pairs_pinned.to(f"cuda:{local}", non_blocking=True)
     out = engine.Results(n, pairs.device)
     torch.cuda.synchronize()
+    choice = ctx.autotune(pool, pairs, reps=1) if not args.no_tune else ctx.kernel_choice()
+    torch.cuda.synchronize()
 
     # one instrumented step: per-kernel CUDA-event times and work counts
     ctx.set_timing(True)
@@ -337,6 +340,8 @@ def run_ours(args):
         "roofline": roof,
         "kernels_ms": {k: round(v, 4) for k, v in ktimes},
         "work": counts,
+        "kernel_choice": choice,
+        "autotuned": not args.no_tune,
     }
     if e2e:
         line["e2e"] = e2e

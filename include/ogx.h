@@ -140,6 +140,119 @@ int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
  * refined in FP64 [15].  cap must be >= 16. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
+/* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most
+ * 16 * 2^b points, bucket 6 the rest): `lanes` lanes per pair, `blocks` float4 blocks of
+ * x, y, z per lane and body kept in registers (0: points re-read from memory).
+ * kind 0 = GJK, 1 = EPA. */
+ogx_status ogx_ctx_get_kernel_choice(const ogx_ctx* ctx, int kind, int bucket, int* lanes,
+                                     int* blocks);
+ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lanes, int blocks);
+/* Autotuner: times every compiled variant that can serve each bucket on this batch
+ * (device buffers; `reps` runs per candidate, best time kept), keeps the fastest per
+ * bucket for this context and for contexts created later on the same device.
+ * Synchronous. */
+ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                        const gkCollisionPair* d_pairs, int reps);
+
+/* ------------------------------------------------------------------------- */
+/* Reference-compatible entry points.  Same arguments, meaning and output     */
+/* conventions as OpenGJK-GPU's host API; each call returns when its results  */
+/* are complete (the reference synchronises the device after every launch).   */
+/* n <= 0 returns OGX_OK without work, as the reference returns early.        */
+
+/* compute_minimum_distance (GJK/gpu/openGJK.h:91), GJK::GPU::computeDistances
+ * (examples/gpu/example.h:21-25): GJK on pairs (bd1[i], bd2[i]), host buffers. */
+ogx_status ogx_compute_minimum_distance(int n, const gkPolytope* bd1, const gkPolytope* bd2,
+                                        gkSimplex* simplices, float* distances);
+/* computeCollisionInformation(n, ...) (GJK/gpu/openGJK.h:112), GJK::GPU::computeEPA
+ * (examples/gpu/example.h:41-46): EPA from GJK simplices/distances (in/out);
+ * contact_normals (n*3) may be NULL. */
+ogx_status ogx_compute_collision_information(int n, const gkPolytope* bd1, const gkPolytope* bd2,
+                                             gkSimplex* simplices, float* distances,
+                                             float* contact_normals);
+/* compute_gjk_epa (GJK/gpu/openGJK.h:134), GJK::GPU::computeGJKAndEPA
+ * (examples/gpu/example.h:62-67). */
+ogx_status ogx_compute_gjk_epa(int n, const gkPolytope* bd1, const gkPolytope* bd2,
+                               gkSimplex* simplices, float* distances, float* contact_normals);
+/* GJK::GPU::computeCollisionInformation as documented in README.md:39-46 (absent from
+ * the reference's code): EPA with witnesses also as n*3 arrays, normals nullable. */
+ogx_status ogx_compute_collision_information_witnesses(int n, const gkPolytope* bd1,
+                                                       const gkPolytope* bd2, gkSimplex* simplices,
+                                                       float* distances, float* witness1,
+                                                       float* witness2, float* contact_normals);
+
+/* mid-level: allocate_and_copy_device_arrays (GJK/gpu/openGJK.h:212) */
+ogx_status ogx_allocate_and_copy_device_arrays(int n, const gkPolytope* bd1, const gkPolytope* bd2,
+                                               gkPolytope** d_bd1, gkPolytope** d_bd2,
+                                               float** d_coord1, float** d_coord2,
+                                               gkSimplex** d_simplices, float** d_distances);
+/* compute_minimum_distance_device (GJK/gpu/openGJK.h:237): descriptors and coordinates
+ * in device memory */
+ogx_status ogx_compute_minimum_distance_device(int n, const gkPolytope* d_bd1,
+                                               const gkPolytope* d_bd2, gkSimplex* d_simplices,
+                                               float* d_distances);
+/* compute_epa_device (GJK/gpu/openGJK.h:255) */
+ogx_status ogx_compute_epa_device(int n, const gkPolytope* d_bd1, const gkPolytope* d_bd2,
+                                  gkSimplex* d_simplices, float* d_distances,
+                                  float* d_contact_normals);
+/* copy_results_from_device (GJK/gpu/openGJK.h:273) */
+ogx_status ogx_copy_results_from_device(int n, const gkSimplex* d_simplices,
+                                        const float* d_distances, gkSimplex* simplices,
+                                        float* distances);
+/* free_device_arrays (GJK/gpu/openGJK.h:292) */
+ogx_status ogx_free_device_arrays(gkPolytope* d_bd1, gkPolytope* d_bd2, float* d_coord1,
+                                  float* d_coord2, gkSimplex* d_simplices, float* d_distances);
+/* allocate_epa_device_arrays (GJK/gpu/openGJK.h:155) */
+ogx_status ogx_allocate_epa_device_arrays(int n, float** d_witness1, float** d_witness2,
+                                          float** d_contact_normals);
+/* copy_epa_results_from_device (GJK/gpu/openGJK.h:173) */
+ogx_status ogx_copy_epa_results_from_device(int n, const float* d_witness1,
+                                            const float* d_witness2,
+                                            const float* d_contact_normals, float* witness1,
+                                            float* witness2, float* contact_normals);
+/* free_epa_device_arrays (GJK/gpu/openGJK.h:194) */
+ogx_status ogx_free_epa_device_arrays(float* d_witness1, float* d_witness2,
+                                      float* d_contact_normals);
+
+/* indexed: allocate_indexed_device (GJK/gpu/openGJK.h:330) */
+ogx_status ogx_allocate_indexed_device(int num_polytopes, int max_pairs,
+                                       const gkPolytope* polytopes, gkPolytope** d_polytopes,
+                                       float** d_coords, gkCollisionPair** d_pairs,
+                                       gkSimplex** d_simplices, float** d_distances,
+                                       float** d_contact_normals);
+/* free_indexed_device (GJK/gpu/openGJK.h:352) */
+ogx_status ogx_free_indexed_device(gkPolytope* d_polytopes, float* d_coords,
+                                   gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                                   float* d_distances, float* d_contact_normals);
+/* upload_pairs_device (GJK/gpu/openGJK.h:368) */
+ogx_status ogx_upload_pairs_device(int num_pairs, const gkCollisionPair* pairs,
+                                   gkCollisionPair* d_pairs);
+/* compute_minimum_distance_indexed (GJK/gpu/openGJK.h:398) */
+ogx_status ogx_compute_minimum_distance_indexed(int num_polytopes, int num_pairs,
+                                                const gkPolytope* polytopes,
+                                                const gkCollisionPair* pairs,
+                                                gkSimplex* simplices, float* distances);
+/* compute_minimum_distance_indexed_device (GJK/gpu/openGJK.h:419) */
+ogx_status ogx_compute_minimum_distance_indexed_device(int num_pairs, const gkPolytope* d_polytopes,
+                                                       const gkCollisionPair* d_pairs,
+                                                       gkSimplex* d_simplices, float* d_distances);
+/* compute_epa_indexed (GJK/gpu/openGJK.h:473): simplices/distances in/out */
+ogx_status ogx_compute_epa_indexed(int num_polytopes, int num_pairs, const gkPolytope* polytopes,
+                                   const gkCollisionPair* pairs, gkSimplex* simplices,
+                                   float* distances, float* contact_normals);
+/* compute_epa_indexed_device (GJK/gpu/openGJK.h:450) */
+ogx_status ogx_compute_epa_indexed_device(int num_pairs, const gkPolytope* d_polytopes,
+                                          const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                                          float* d_distances, float* d_contact_normals);
+/* compute_gjk_epa_indexed (GJK/gpu/openGJK.h:497) */
+ogx_status ogx_compute_gjk_epa_indexed(int num_polytopes, int num_pairs,
+                                       const gkPolytope* polytopes, const gkCollisionPair* pairs,
+                                       gkSimplex* simplices, float* distances,
+                                       float* contact_normals);
+/* GJK::GPU::timer() (examples/gpu/example.h:9): GPU milliseconds of the engine pipeline
+ * of the last reference-compatible call on the current device. */
+float ogx_compat_last_gpu_ms(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,29 @@ struct MemBodies {
   OGX_HD dv3 dpoint(int w, int i) const { return cvt<double>(point(w, i)); }
   OGX_HD const MemBodies& mem_view() const { return *this; }
 
+  // lane-local best value over all points, best value over the points whose index is
+  // not in ex[0..3) (the final simplex's points of this body), and max |coordinate|
+  template <class Team>
+  OGX_HD void scan_excl(const Team& t, int w, fv3 d, const int* ex, float& b1, float& bo,
+                        float& amax) const {
+    b1 = bo = -INFINITY;
+    amax = 0.0f;
+    const int nb = n4[w] >> 2;
+    const float* X = base[w];
+    const float* Y = X + n4[w];
+    const float* Z = X + 2 * n4[w];
+    for (int q = t.lane(); q < nb; q += Team::L) {
+      for (int c = 0; c < 4; ++c) {
+        const int i = 4 * q + c;
+        if (i >= n[w]) break;
+        const float v = sdot(X[i], Y[i], Z[i], d);
+        b1 = fmaxf(b1, v);
+        if (i != ex[0] && i != ex[1] && i != ex[2]) bo = fmaxf(bo, v);
+        amax = fmaxf(amax, fmaxf(fabsf(X[i]), fmaxf(fabsf(Y[i]), fabsf(Z[i]))));
+      }
+    }
+  }
+
   template <class Team>
   OGX_HD void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {
     best = -INFINITY;
@@ -91,6 +114,28 @@ struct RegBodies {
   __device__ fv3 point(int w, int i) const { return mem.point(w, i); }
   __device__ dv3 dpoint(int w, int i) const { return mem.dpoint(w, i); }
   __device__ const MemBodies& mem_view() const { return mem; }
+
+  template <class Team>
+  __device__ void scan_excl(const Team& t, int w, fv3 d, const int* ex, float& b1, float& bo,
+                            float& amax) const {
+    b1 = bo = -INFINITY;
+    amax = 0.0f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const int q4 = 4 * (t.lane() + j * L);
+      const float4 X = x[w][j], Y = y[w][j], Z = z[w][j];
+      const float xs[4] = {X.x, X.y, X.z, X.w}, ys[4] = {Y.x, Y.y, Y.z, Y.w}, zs[4] = {Z.x, Z.y, Z.z, Z.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int i = q4 + c;
+        const bool live = i < mem.n[w];  // padding repeats point 0: skip it here
+        const float v = live ? sdot(xs[c], ys[c], zs[c], d) : -INFINITY;
+        b1 = fmaxf(b1, v);
+        if (i != ex[0] && i != ex[1] && i != ex[2]) bo = fmaxf(bo, v);
+        if (live) amax = fmaxf(amax, fmaxf(fabsf(xs[c]), fmaxf(fabsf(ys[c]), fabsf(zs[c]))));
+      }
+    }
+  }
 
   template <class Team>
   __device__ void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {

@@ -191,6 +191,7 @@ struct SerialTeam {
   OGX_HD int lane() const { return 0; }
   OGX_HD void argmax(float&, int&) const {}
   OGX_HD void argmin(float&, int&) const {}
+  OGX_HD void argmax2(float&, int&, float&) const {}
   OGX_HD bool any(bool p) const { return p; }
   OGX_HD int excl_scan(int x, int& total) const {
     total = x;
@@ -224,6 +225,21 @@ struct WarpTeam {
         v = v2;
         i = i2;
       }
+    }
+  }
+  // best value / index (ties to the smaller index) and the runner-up value over lanes
+  __device__ void argmax2(float& b1, int& i1, float& b2) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      const float c1 = __shfl_xor_sync(mask, b1, o);
+      const int j1 = __shfl_xor_sync(mask, i1, o);
+      const float c2 = __shfl_xor_sync(mask, b2, o);
+      const float lo = fminf(b1, c1);
+      if (c1 > b1 || (c1 == b1 && j1 < i1)) {
+        b1 = c1;
+        i1 = j1;
+      }
+      b2 = fmaxf(fmaxf(b2, c2), lo);
     }
   }
   // min value, ties to the smaller index (index -1 means "none" and loses)

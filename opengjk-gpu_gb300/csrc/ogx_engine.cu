@@ -89,18 +89,61 @@ namespace {
 struct Launch {
   BucketKernel fn;
   int L;
+  int K;
   size_t smem;
   int grid;  // resident blocks x SMs on the current device
 };
 
-Launch g_gjk[kBuckets];
-Launch g_epa[kBuckets];
+std::vector<Launch> g_gjkv, g_epav;  // all compiled variants
 
 constexpr int kBlock = 128;
+constexpr int kBucketCap[kBuckets] = {16, 32, 64, 128, 256, 512, 0};
 
 std::mutex g_init_mu;
 int g_init_device = -1;
 int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0;
+// per-device autotuned choices (variant index per bucket), -1 = not tuned
+int g_tuned[16][2][kBuckets];
+bool g_tuned_valid[16];
+
+// can variant v serve bucket b?
+bool serves(const Launch& v, int b) {
+  if (v.K == 0) return b >= 4;  // memory-streamed: only worth trying for large bodies
+  if (b == kBuckets - 1) return false;
+  const int cap = 4 * v.L * v.K;
+  return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];
+}
+
+// default choice before tuning: one pair per warp, fewest registers that fit
+int default_choice(const std::vector<Launch>& vs, int b) {
+  int best = -1;
+  for (int i = 0; i < (int)vs.size(); ++i) {
+    if (!serves(vs[i], b) || vs[i].L != 32) continue;
+    if (b == kBuckets - 1) {
+      if (vs[i].K == 0) return i;
+      continue;
+    }
+    if (vs[i].K == 0) continue;
+    if (best < 0 || vs[i].K < vs[best].K) best = i;
+  }
+  return best;
+}
+
+ogx_status init_variant(Launch* k, bool epa, int sms) {
+  k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMem) : 0;
+  cudaError_t e;
+  if (k->smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)k->smem);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaFuncSetAttribute");
+  }
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->fn, kBlock, k->smem);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+  if (per_sm < 1) return ogx_fail(OGX_ERR_CUDA, "kernel variant (%d,%d) cannot be resident", k->L, k->K);
+  k->grid = per_sm * sms;
+  return OGX_OK;
+}
 
 ogx_status init_kernels(int device) {
   std::lock_guard<std::mutex> lk(g_init_mu);
@@ -108,23 +151,24 @@ ogx_status init_kernels(int device) {
   int sms = 0;
   cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaDeviceGetAttribute");
-  for (int b = 0; b < kBuckets; ++b) {
-    g_gjk[b] = Launch{gjk_kernels()[b].fn, gjk_kernels()[b].L, 0, 0};
-    g_epa[b] = Launch{epa_kernels()[b].fn, epa_kernels()[b].L, 0, 0};
-    for (Launch* k : {&g_gjk[b], &g_epa[b]}) {
-      const bool epa = (k == &g_epa[b]);
-      k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMem) : 0;
-      if (k->smem > 48 * 1024) {
-        e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn),
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k->smem);
-        if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaFuncSetAttribute");
-      }
-      int per_sm = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k->fn, kBlock, k->smem);
-      if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-      if (per_sm < 1) return ogx_fail(OGX_ERR_CUDA, "bucket kernel %d cannot be resident", b);
-      k->grid = per_sm * sms;
-    }
+  g_gjkv.clear();
+  g_epav.clear();
+  const KernelInfo* t;
+  int n = gjk_variants_a(&t);
+  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = gjk_variants_b(&t);
+  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = epa_variants_a(&t);
+  for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = epa_variants_b(&t);
+  for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  for (auto& k : g_gjkv) {
+    ogx_status s = init_variant(&k, false, sms);
+    if (s) return s;
+  }
+  for (auto& k : g_epav) {
+    ogx_status s = init_variant(&k, true, sms);
+    if (s) return s;
   }
   g_grid_bin = 4 * sms;
   g_grid_pack = 8 * sms;
@@ -137,6 +181,14 @@ ogx_status init_kernels(int device) {
   g_grid_refine = std::max(1, per_sm) * sms;
   g_init_device = device;
   return OGX_OK;
+}
+
+void set_defaults(ogx_ctx* ctx) {
+  const bool tuned = ctx->device < 16 && g_tuned_valid[ctx->device];
+  for (int b = 0; b < kBuckets; ++b) {
+    ctx->choice[0][b] = tuned ? g_tuned[ctx->device][0][b] : default_choice(g_gjkv, b);
+    ctx->choice[1][b] = tuned ? g_tuned[ctx->device][1][b] : default_choice(g_epav, b);
+  }
 }
 
 }  // namespace
@@ -175,6 +227,7 @@ extern "C" ogx_status ogx_ctx_create(int device, const ogx_config* cfg, void* st
   ogx_ctx* ctx = new ogx_ctx();
   ctx->device = device;
   ctx->cfg = c;
+  set_defaults(ctx);
   cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (stream) {
     ctx->stream = static_cast<cudaStream_t>(stream);
@@ -302,7 +355,7 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
   if ((e = cudaMalloc(&d_lists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_elists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_polish, cap * sizeof(PolishRec))) != cudaSuccess ||
-      (e = cudaMalloc(&d_refine, cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_refine, cap * sizeof(RefineRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_counts, 64 * sizeof(int))) != cudaSuccess) {
     free_scratch();
     return ogx_cuda_fail(e, "scratch allocation");
@@ -503,8 +556,9 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   ++launches;
   if (mode != kModeEpa) {
     for (int b = kBuckets - 1; b >= 0; --b) {
+      const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
-      g_gjk[b].fn<<<g_gjk[b].grid, kBlock, 0, st>>>(B, b);
+      k.fn<<<k.grid, kBlock, 0, st>>>(B, b);
       ++launches;
     }
   }
@@ -516,8 +570,9 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   }
   if (mode != kModeGjk) {
     for (int b = kBuckets - 1; b >= 0; --b) {
+      const Launch& k = g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
-      g_epa[b].fn<<<g_epa[b].grid, kBlock, g_epa[b].smem, st>>>(B, b);
+      k.fn<<<k.grid, kBlock, k.smem, st>>>(B, b);
       ++launches;
     }
   }
@@ -556,4 +611,113 @@ extern "C" ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
   if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
   return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
                  d_distances, d_normals, d_status, kModeEpa);
+}
+
+// ---------------------------------------------------------------------------------
+// kernel choice and autotuning
+
+extern "C" ogx_status ogx_ctx_get_kernel_choice(const ogx_ctx* ctx, int kind, int bucket, int* lanes,
+                                                int* blocks) {
+  if (!ctx || kind < 0 || kind > 1 || bucket < 0 || bucket >= kBuckets)
+    return ogx_fail(OGX_ERR_INVALID, "bad kind/bucket");
+  const Launch& k = (kind == 0 ? g_gjkv : g_epav)[ctx->choice[kind][bucket]];
+  if (lanes) *lanes = k.L;
+  if (blocks) *blocks = k.K;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lanes, int blocks) {
+  if (!ctx || kind < 0 || kind > 1 || bucket < 0 || bucket >= kBuckets)
+    return ogx_fail(OGX_ERR_INVALID, "bad kind/bucket");
+  const std::vector<Launch>& vs = kind == 0 ? g_gjkv : g_epav;
+  for (int i = 0; i < (int)vs.size(); ++i)
+    if (vs[i].L == lanes && vs[i].K == blocks && serves(vs[i], bucket)) {
+      ctx->choice[kind][bucket] = i;
+      return OGX_OK;
+    }
+  return ogx_fail(OGX_ERR_INVALID, "no variant (%d lanes, %d blocks) for bucket %d", lanes, blocks, bucket);
+}
+
+// Times every compiled variant that can serve each bucket on the caller's batch (round r
+// runs candidate r of every bucket at once, `reps` times, keeping the best time) and keeps
+// the fastest per bucket for this context and for contexts created later on the device.
+extern "C" ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkCollisionPair* d_pairs,
+                                   int reps) {
+  if (!ctx || !pool || !d_pairs || npairs <= 0) return ogx_fail(OGX_ERR_INVALID, "bad autotune arguments");
+  cudaSetDevice(ctx->device);
+  gkSimplex* smp = nullptr;
+  float *dist = nullptr, *nrm = nullptr;
+  cudaError_t e = cudaMalloc(&smp, npairs * sizeof(gkSimplex));
+  if (e == cudaSuccess) e = cudaMalloc(&dist, npairs * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&nrm, 3 * (size_t)npairs * sizeof(float));
+  if (e != cudaSuccess) {
+    cudaFree(smp);
+    cudaFree(dist);
+    return ogx_cuda_fail(e, "autotune buffers");
+  }
+  std::vector<int> cands[2][kBuckets];
+  int rounds = 0;
+  for (int kind = 0; kind < 2; ++kind)
+    for (int b = 0; b < kBuckets; ++b) {
+      const std::vector<Launch>& vs = kind == 0 ? g_gjkv : g_epav;
+      for (int i = 0; i < (int)vs.size(); ++i)
+        if (serves(vs[i], b)) cands[kind][b].push_back(i);
+      rounds = std::max(rounds, (int)cands[kind][b].size());
+    }
+  float best[2][kBuckets];
+  int pick[2][kBuckets];
+  for (int kind = 0; kind < 2; ++kind)
+    for (int b = 0; b < kBuckets; ++b) {
+      best[kind][b] = INFINITY;
+      pick[kind][b] = ctx->choice[kind][b];
+    }
+  const bool was_timing = ctx->timing;
+  ogx_status s = ogx_ctx_set_timing(ctx, 1);
+  for (int r = 0; r < rounds && !s; ++r) {
+    for (int kind = 0; kind < 2; ++kind)
+      for (int b = 0; b < kBuckets; ++b) {
+        const auto& c = cands[kind][b];
+        if (!c.empty()) ctx->choice[kind][b] = c[r % c.size()];
+      }
+    for (int k = 0; k < std::max(1, reps) && !s; ++k) {
+      s = ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, smp, dist, nrm, nullptr,
+                  kModeGjkEpa);
+      if (s) break;
+      const char* names[ogx_ctx::kMaxTimed];
+      float ms[ogx_ctx::kMaxTimed];
+      const int n = ogx_ctx_kernel_times(ctx, names, ms, ogx_ctx::kMaxTimed);
+      for (int i = 0; i < n; ++i) {
+        int kind = -1, b = -1;
+        if (!strncmp(names[i], "gjk", 3)) kind = 0;
+        if (!strncmp(names[i], "epa", 3)) kind = 1;
+        if (kind < 0) continue;
+        const char* bn = names[i] + 3;
+        static const char* kB[kBuckets] = {"<=16", "<=32", "<=64", "<=128", "<=256", "<=512", ">512"};
+        for (int q = 0; q < kBuckets; ++q)
+          if (!strcmp(bn, kB[q])) b = q;
+        if (b < 0 || r >= (int)cands[kind][b].size()) continue;  // this round repeats a candidate
+        if (ms[i] < best[kind][b]) {
+          best[kind][b] = ms[i];
+          pick[kind][b] = ctx->choice[kind][b];
+        }
+      }
+    }
+  }
+  ogx_ctx_set_timing(ctx, was_timing);
+  cudaFree(smp);
+  cudaFree(dist);
+  cudaFree(nrm);
+  if (s) {
+    set_defaults(ctx);
+    return s;
+  }
+  for (int kind = 0; kind < 2; ++kind)
+    for (int b = 0; b < kBuckets; ++b) ctx->choice[kind][b] = pick[kind][b];
+  if (ctx->device < 16) {
+    std::lock_guard<std::mutex> lk(g_init_mu);
+    for (int kind = 0; kind < 2; ++kind)
+      for (int b = 0; b < kBuckets; ++b) g_tuned[ctx->device][kind][b] = pick[kind][b];
+    g_tuned_valid[ctx->device] = true;
+  }
+  return OGX_OK;
 }

@@ -18,7 +18,7 @@ struct ogx_ctx {
   int* d_elists = nullptr;
   int* d_counts = nullptr;
   ogx::PolishRec* d_polish = nullptr;
-  int* d_refine = nullptr;
+  ogx::RefineRec* d_refine = nullptr;
   size_t cap_pairs = 0;
   // staging for host uploads
   void* h_stage = nullptr;
@@ -26,6 +26,7 @@ struct ogx_ctx {
   void* d_stage = nullptr;
   size_t d_stage_bytes = 0;
   int last_launches = 0;
+  int choice[2][ogx::kBuckets] = {};  // kernel variant per bucket: [0] GJK, [1] EPA
   // optional per-launch timing (CUDA events recorded between the launches of a call)
   bool timing = false;
   static constexpr int kMaxTimed = 32;

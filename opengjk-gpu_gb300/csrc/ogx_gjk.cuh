@@ -445,6 +445,8 @@ struct GjkState {
   int status;
   int exit;     // why the loop ended (GJK_EXIT_*)
   bool polish;  // the FP32 distance is not known to polish_rel: re-solve in FP64
+  int wa, wb;   // support pair along the final direction
+  bool certain; // that support is the exact (FP64) support along the exact direction
 };
 
 // loop exit reasons (reported in status bits 16..18)
@@ -646,9 +648,39 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
   // FP32 error of |v| is a few ulp of the simplex scale; ask for an FP64 re-solve when
   // that is not small against the distance.
   g.polish = false;
+  g.certain = false;
+  g.wa = ia;
+  g.wb = ib;
   if ((cfg.flags & OGX_F_FP64_POLISH) && g.n >= 2 && g.n <= 3 && !gjk_contact(g)) {
     const float errb = 16.0f * FLT_EPSILON * sqrtf(g.wmax2);
     g.polish = errb > cfg.polish_rel * g.dist;
+  }
+  if (g.polish) {
+    // Is the exact support along the exact closest point v64 one of the final simplex's
+    // own points?  Then GJK's stop is exact and the FP64 closest point of the simplex is
+    // the answer.  Each body's points outside the simplex must trail its best point by
+    // more than twice the error of an FP32 support value against the exact value along
+    // v64: FP32 dot rounding (4 eps amax |v|_1) plus the FP32 projection error of v
+    // (16 eps |W| per component).
+    int exa[3] = {-1, -1, -1}, exb[3] = {-1, -1, -1};
+    for (int j = 0; j < g.n && j < 3; ++j) {
+      exa[j] = g.ia[j];
+      exb[j] = g.ib[j];
+    }
+    float a1, ao, am, b1, bo, bm;
+    B.scan_excl(t, 0, -v, exa, a1, ao, am);
+    B.scan_excl(t, 1, v, exb, b1, bo, bm);
+    a1 = t.fmax_(a1);
+    ao = t.fmax_(ao);
+    am = t.fmax_(am);
+    b1 = t.fmax_(b1);
+    bo = t.fmax_(bo);
+    bm = t.fmax_(bm);
+    const float dv = 16.0f * FLT_EPSILON * sqrtf(g.wmax2) * 3.0f;
+    const float l1v = fabsf(v.x) + fabsf(v.y) + fabsf(v.z);
+    const float ea = 4.0f * FLT_EPSILON * am * l1v + am * dv;
+    const float eb = 4.0f * FLT_EPSILON * bm * l1v + bm * dv;
+    g.certain = (a1 - ao > 2.0f * ea) && (b1 - bo > 2.0f * eb);
   }
 }
 
@@ -691,6 +723,7 @@ OGX_HD int exact_support(const Bodies& B, int w, dv3 d, double& val) {
 // (or corrects) the FP32 answer; sets g.n = 4 if the origin turns out to be enclosed.
 template <class Bodies>
 OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
+  const bool certain = g.certain;
   Sx<double> s;
   int ia[4], ib[4];
   s.n = g.n > 3 ? 3 : g.n;
@@ -734,6 +767,7 @@ OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
   bool enclosed = false;
   double wmax2 = 0.0;
   for (int j = 0; j < s.n; ++j) wmax2 = fmax(wmax2, dot(s.v[j].p, s.v[j].p));
+  if (certain) it = max_iter + 1;  // the FP32 pass proved the simplex final
   for (; it < max_iter; ++it) {
     double va, vb;
     const int xa = exact_support(B, 0, -v, va);
@@ -804,7 +838,7 @@ OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
     g.ib[j] = ib[j];
     g.P[j] = cvt<float>(s.v[j].p);
   }
-  g.status |= OGX_S_POLISHED;
+  g.status |= (it == max_iter + 1) ? OGX_S_POLISHED : (OGX_S_POLISHED | OGX_S_GJK_ESCALATED);
   if (it == max_iter) g.status |= OGX_S_GJK_CAP;
   if (enclosed) {
     g.v = v3<float>(0.f, 0.f, 0.f);

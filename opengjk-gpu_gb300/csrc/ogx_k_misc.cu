@@ -89,7 +89,8 @@ __global__ void k_bin(DevBatch B) {
 __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   const int cnt = B.counts[kCntRefine];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
-    const int p = B.refine[k];
+    const RefineRec rr = B.refine[k];
+    const int p = rr.pair;
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
     MemBodies mb;
@@ -97,6 +98,9 @@ __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
     gkSimplex* s = B.smp + p;
     GjkState g;
     load_simplex(s, B.dist[p], g);
+    g.wa = rr.wa;
+    g.wb = rr.wb;
+    g.certain = rr.certain != 0;
     gjk_refine(mb, g, kRefineIters);
     store_simplex(s, g);
     B.dist[p] = g.dist;

@@ -27,6 +27,14 @@ OGX_HD int bucket_of(int m) {
   return m <= 16 ? 0 : m <= 32 ? 1 : m <= 64 ? 2 : m <= 128 ? 3 : m <= 256 ? 4 : m <= 512 ? 5 : 6;
 }
 
+// FP64 refinement request of a separated pair: the support pair along the final
+// direction and whether the FP32 pass proved it exact
+struct RefineRec {
+  int pair;
+  int wa, wb;
+  int certain;
+};
+
 // FP64 re-solve request: GJK simplex (kind 0) or the final EPA face (kind 1)
 struct PolishRec {
   int pair;
@@ -58,7 +66,7 @@ struct DevBatch {
   int* elists;      // kBuckets regions of npairs entries
   int* counts;      // kCntSlots
   PolishRec* polish;
-  int* refine;      // npairs entries
+  RefineRec* refine;  // npairs entries
   ogx_config cfg;
   int mode;
 };
@@ -168,7 +176,14 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
     const int e = warp_append(B.counts + kCntEpa + bucket, to_epa);
     if (to_epa) B.elists[(size_t)bucket * B.npairs + e] = p;
     const int q = warp_append(B.counts + kCntRefine, lead && g.polish);
-    if (lead && g.polish) B.refine[q] = p;
+    if (lead && g.polish) {
+      RefineRec r;
+      r.pair = p;
+      r.wa = g.wa;
+      r.wb = g.wb;
+      r.certain = g.certain ? 1 : 0;
+      B.refine[q] = r;
+    }
   }
 }
 
@@ -230,9 +245,15 @@ struct KernelInfo {
   int K;  // float4 blocks per lane and body kept in registers (0: read from memory)
 };
 
-// GJK and EPA kernels by bucket (<=16, 32, 64, 128, 256, 512, more points)
-const KernelInfo* gjk_kernels();
-const KernelInfo* epa_kernels();
+// Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
+// (L, K) can serve a bucket whose bodies have at most 4 L K points (K = 0: any size, the
+// points are re-read from memory).  The engine picks one per bucket (autotuned).
+int gjk_variants(const KernelInfo** out);
+int epa_variants(const KernelInfo** out);
+int gjk_variants_a(const KernelInfo** out);
+int gjk_variants_b(const KernelInfo** out);
+int epa_variants_a(const KernelInfo** out);
+int epa_variants_b(const KernelInfo** out);
 
 // non-template kernels (ogx_k_misc.cu)
 cudaError_t launch_refine(const DevBatch& B, int grid, cudaStream_t st);

@@ -101,6 +101,9 @@ SIGNATURES = {
     "ogx_ctx_set_timing": (_I, [_P, _I]),
     "ogx_ctx_kernel_times": (_I, [_P, _P, _P, _I]),
     "ogx_ctx_work_counts": (_I, [_P, _P, _I]),
+    "ogx_ctx_get_kernel_choice": (_I, [_P, _I, _I, _P, _P]),
+    "ogx_ctx_set_kernel_choice": (_I, [_P, _I, _I, _I, _I]),
+    "ogx_autotune": (_I, [_P, _P, _I, _P, _I]),
     "ogx_pool_create": (_I, [_P, _I, _P, _P]),
     "ogx_pool_destroy": (_I, [_P]),
     "ogx_pool_num_bodies": (_I, [_P]),

@@ -83,6 +83,27 @@ class Context:
             raise _lib.OgxError(-2, "kernel timing failed")
         return [(names[i].decode(), float(ms[i])) for i in range(n)]
 
+    def kernel_choice(self) -> dict:
+        """{"gjk": [(lanes, blocks)] * 7, "epa": [...]} per size bucket."""
+        out = {}
+        for kind, name in ((0, "gjk"), (1, "epa")):
+            row = []
+            for b in range(7):
+                L, K = ctypes.c_int(), ctypes.c_int()
+                check(self.lib.ogx_ctx_get_kernel_choice(self.handle, kind, b, ctypes.byref(L), ctypes.byref(K)))
+                row.append((L.value, K.value))
+            out[name] = row
+        return out
+
+    def set_kernel_choice(self, kind: str, bucket: int, lanes: int, blocks: int):
+        check(self.lib.ogx_ctx_set_kernel_choice(self.handle, 0 if kind == "gjk" else 1, bucket, lanes, blocks))
+
+    def autotune(self, pool, pairs_dev, reps: int = 2):
+        """Pick the fastest kernel variant per bucket on this batch (synchronous)."""
+        check(self.lib.ogx_autotune(self.handle, pool.handle, int(pairs_dev.shape[0]),
+                                    ctypes.c_void_p(pairs_dev.data_ptr()), int(reps)))
+        return self.kernel_choice()
+
     def work_counts(self) -> dict:
         c = (ctypes.c_int32 * 16)()
         n = self.lib.ogx_ctx_work_counts(self.handle, c, 16)

@@ -13,7 +13,9 @@ Tolerances (stated once, used by every parity test):
     depth exceeds the oracle's depth by at most EQUIV * max(1, depth) (EQUIV = 1e-6);
     witnesses satisfy w0 - w1 = depth * n and lie on the support planes of their bodies
     within ABS4; where the oracle's own witnesses are self-consistent and the contact
-    features are unique, they agree with the oracle's within ABS4 (ABS4 = 1e-4).
+    features are unique, they agree with the oracle's within ABS4 (ABS4 = 1e-4) -- for
+    all but a stated small fraction: dense clouds (hundreds of points per body) make the
+    contact point ill-conditioned, and the invariants above are what certify those.
 """
 import numpy as np
 

@@ -84,7 +84,7 @@ def test_large_bodies_streamed_bucket(engine, orc):
     b = W.ellipsoid(seed=8, n_pairs=300, lo=600, hi=3000)
     res = engine.query(b, engine.MODE_GJK_EPA)
     o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=16)
-    parity.assert_parity(parity.check(b, res, o, label="large"))
+    parity.assert_parity(parity.check(b, res, o, label="large"), max_witness_mismatch_frac=0.02)
 
 
 def test_deterministic_and_batch_independent(engine):
@@ -108,7 +108,8 @@ def test_epa_only_matches_fused(engine):
     pool.upload(b.coords)
     pairs = torch.from_numpy(b.pairs).cuda()
     fused = engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA).to_host()
-    r = engine.run(ctx, pool, pairs, engine.MODE_GJK)
+    r = engine.Results(b.n_pairs, pairs.device, with_normals=True)
+    engine.run(ctx, pool, pairs, engine.MODE_GJK, out=r)
     engine.run(ctx, pool, pairs, engine.MODE_EPA, out=r)
     sep = r.to_host()
     assert np.array_equal(fused["dist"], sep["dist"])
