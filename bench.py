@@ -228,8 +228,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         return
 
-    for _ in range(args.warmup):
-        engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
     launches_per_step = ctx.last_launches
     torch.cuda.synchronize()
     if world > 1:
@@ -238,8 +239,9 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
-        for _ in range(args.steps):
-            engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps

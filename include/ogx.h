@@ -137,7 +137,8 @@ ogx_status ogx_ctx_set_timing(ogx_ctx* ctx, int on);
 int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
 /* Work counts of the last call (waits for it): pairs per GJK bucket [0, 7), contacts
  * per EPA bucket [7, 14), EPA faces re-solved in FP64 [14], pairs whose GJK result was
- * refined in FP64 [15].  cap must be >= 16. */
+ * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16].
+ * cap must be >= 17. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 /* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most

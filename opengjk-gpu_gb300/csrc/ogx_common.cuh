@@ -192,6 +192,7 @@ struct SerialTeam {
   OGX_HD void argmax(float&, int&) const {}
   OGX_HD void argmin(float&, int&) const {}
   OGX_HD void argmax2(float&, int&, float&) const {}
+  OGX_HD void argmax_d(double&, int&) const {}
   OGX_HD bool any(bool p) const { return p; }
   OGX_HD int excl_scan(int x, int& total) const {
     total = x;
@@ -220,6 +221,18 @@ struct WarpTeam {
 #pragma unroll
     for (int o = L / 2; o > 0; o >>= 1) {
       const float v2 = __shfl_xor_sync(mask, v, o);
+      const int i2 = __shfl_xor_sync(mask, i, o);
+      if (v2 > v || (v2 == v && i2 < i)) {
+        v = v2;
+        i = i2;
+      }
+    }
+  }
+  // FP64 max value, ties to the smaller index
+  __device__ void argmax_d(double& v, int& i) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      const double v2 = __shfl_xor_sync(mask, v, o);
       const int i2 = __shfl_xor_sync(mask, i, o);
       if (v2 > v || (v2 == v && i2 < i)) {
         v = v2;

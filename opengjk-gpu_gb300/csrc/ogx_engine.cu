@@ -250,7 +250,9 @@ void ogx_ctx::free_scratch() {
   cudaFree(d_polish);
   cudaFree(d_counts);
   cudaFree(d_refine);
+  cudaFree(d_refine_full);
   d_refine = nullptr;
+  d_refine_full = nullptr;
   d_lists = d_elists = d_counts = nullptr;
   d_polish = nullptr;
   cap_pairs = 0;
@@ -356,6 +358,7 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
       (e = cudaMalloc(&d_elists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_polish, cap * sizeof(PolishRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine, cap * sizeof(RefineRec))) != cudaSuccess ||
+      (e = cudaMalloc(&d_refine_full, cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_counts, 64 * sizeof(int))) != cudaSuccess) {
     free_scratch();
     return ogx_cuda_fail(e, "scratch allocation");
@@ -538,6 +541,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.counts = ctx->d_counts;
   B.polish = ctx->d_polish;
   B.refine = ctx->d_refine;
+  B.refine_full = ctx->d_refine_full;
   B.cfg = ctx->cfg;
   B.mode = mode;
   cudaStream_t st = ctx->stream;
@@ -564,9 +568,9 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   }
   if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("refine");
-    e = launch_refine(B, g_grid_refine, st);
+    e = launch_refine(B, g_grid_refine, g_grid_pack, st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
-    ++launches;
+    launches += 2;
   }
   if (mode != kModeGjk) {
     for (int b = kBuckets - 1; b >= 0; --b) {

@@ -19,6 +19,7 @@ struct ogx_ctx {
   int* d_counts = nullptr;
   ogx::PolishRec* d_polish = nullptr;
   ogx::RefineRec* d_refine = nullptr;
+  int* d_refine_full = nullptr;
   size_t cap_pairs = 0;
   // staging for host uploads
   void* h_stage = nullptr;

@@ -23,6 +23,7 @@
 #pragma once
 
 #include "ogx_common.cuh"
+#include "ogx_subdist.cuh"
 
 namespace ogx {
 
@@ -502,19 +503,44 @@ OGX_HD void simplex_weights(const GjkState& g, float* lam) {
   }
 }
 
+// FP64 re-run of one sub-distance step on the exact Minkowski points (cold path: taken
+// when an FP32 decision of the step falls inside its rounding bound).  Returns the new
+// slot order in `order` and the new direction.
+#if defined(__CUDACC__)
+__noinline__
+#endif
+OGX_HD int escalate_step(const MemBodies B, int n, const int* ia, const int* ib, fv3 vold, int* order, fv3* vout) {
+  Sx<double> sd;
+  sd.n = n;
+  for (int j = 0; j < n; ++j) {
+    sd.v[j].p = B.dpoint(0, ia[j]) - B.dpoint(1, ib[j]);
+    sd.v[j].k = j;
+  }
+  dv3 vd = cvt<double>(vold);
+  Unc ud{false};
+  subdistance(sd, vd, ud);
+  for (int j = 0; j < sd.n; ++j) order[j] = sd.v[j].k;
+  *vout = cvt<float>(vd);
+  return sd.n;
+}
+
 template <class Team, class Bodies>
 OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g) {
   const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
   const fv3 a0 = B.point(0, 0), b0 = B.point(1, 0);
   fv3 v = a0 - b0;
-  g.n = 1;
-  g.P[0] = v;
-  g.ia[0] = 0;
-  g.ib[0] = 0;
+  // simplex in registers: slots 0..3, newest last; every index below is unrolled
+  fv3 P[4];
+  int IA[4], IB[4];
+  P[0] = v;
+  P[1] = P[2] = P[3] = v;
+  IA[0] = IB[0] = 0;
+  IA[1] = IA[2] = IA[3] = IB[1] = IB[2] = IB[3] = -1;
+  int n = 1;
   g.status = 0;
   g.exit = 0;
-  g.wmax2 = 0.0f;
+  float wmax2 = 0.0f;
   fv3 sa = a0, sb = b0;
   int ia = 0, ib = 0;
   const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
@@ -560,67 +586,90 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
     }
     if (!reftol) {
       bool dup = false;
-      for (int j = 0; j < g.n; ++j) dup |= (g.ia[j] == ia && g.ib[j] == ib);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dup |= (j < n) && IA[j] == ia && IB[j] == ib;
       if (dup) {
         g.exit = GJK_EXIT_DUPLICATE;
         break;
       }
     }
-    g.P[g.n] = w;
-    g.ia[g.n] = ia;
-    g.ib[g.n] = ib;
-    g.n++;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j == n) {
+        P[j] = w;
+        IA[j] = ia;
+        IB[j] = ib;
+      }
+    ++n;
 
-    Sx<float> sf;
-    sf.n = g.n;
-    for (int j = 0; j < g.n; ++j) {
-      sf.v[j].p = g.P[j];
-      sf.v[j].k = j;
+    StepIn S;
+    uint32_t bits, unc;
+    step_predicates(n, P, S, bits, unc);
+    SubOut o = step_decide(n, bits);
+    // degenerate spans make the projection itself unreliable
+    if (o.kind == SO_LINE) {
+      const float ge = o.a == 0 ? S.g[0][0] : (o.a == 1 ? S.g[1][1] : S.g[2][2]);
+      const float lq = l1(S.q1);
+      if (!(ge > 64.0f * FLT_EPSILON * FLT_EPSILON * lq * lq)) unc |= o.used | 1u;
+    } else if (o.kind == SO_PLANE) {
+      const fv3 ea = o.a == 0 ? S.e[0] : (o.a == 1 ? S.e[1] : S.e[2]);
+      const fv3 eb = o.b == 0 ? S.e[0] : (o.b == 1 ? S.e[1] : S.e[2]);
+      const int pab = (o.a < o.b ? o.a : o.b) * 3 + (o.a < o.b ? o.b : o.a);
+      const fv3 c = pab == 1 ? S.c01 : (pab == 2 ? S.c02 : S.c12);
+      const float bc = 32.0f * FLT_EPSILON * l1(ea) * l1(eb);
+      if (!(dot(c, c) > bc * bc)) unc |= o.used | 1u;
     }
-    Unc u{false};
-    fv3 nvf = v;
-    subdistance(sf, nvf, u);
-    int order[4] = {0, 1, 2, 3};
-    int nn = sf.n;
-    if (u.hit && escalate) {
-      Sx<double> sd;
-      sd.n = g.n;
-      for (int j = 0; j < g.n; ++j) {
-        sd.v[j].p = B.dpoint(0, g.ia[j]) - B.dpoint(1, g.ib[j]);
-        sd.v[j].k = j;
+    int nn;
+    fv3 P2[3];
+    int A2[3], B2[3];
+    if ((unc & o.used) != 0u && escalate) {
+      int order[4] = {0, 1, 2, 3};
+      int ias[4], ibs[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        ias[j] = IA[j];
+        ibs[j] = IB[j];
       }
-      dv3 vd = cvt<double>(v);
-      Unc ud{false};
-      subdistance(sd, vd, ud);
-      nn = sd.n;
-      for (int j = 0; j < nn; ++j) order[j] = sd.v[j].k;
-      v = cvt<float>(vd);
+      fv3 vd;
+      nn = escalate_step(B.mem_view(), n, ias, ibs, v, order, &vd);
+      v = vd;
       g.status |= OGX_S_GJK_ESCALATED;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int sj = order[j];
+        P2[j] = sel3(sj, P[0], P[1], P[2], P[3]);
+        A2[j] = seli(sj, IA[0], IA[1], IA[2], IA[3]);
+        B2[j] = seli(sj, IB[0], IB[1], IB[2], IB[3]);
+      }
     } else {
-      for (int j = 0; j < nn; ++j) order[j] = sf.v[j].k;
-      v = nvf;
-    }
-    {
-      fv3 P2[4];
-      int a2[4], b2[4];
-      for (int j = 0; j < nn; ++j) {
-        P2[j] = g.P[order[j]];
-        a2[j] = g.ia[order[j]];
-        b2[j] = g.ib[order[j]];
+      v = step_direction(n, S, o, v);
+      // slots are numbered for the tetrahedron (newest = 3); map for smaller steps
+      nn = o.n;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const int sj = (o.s[j] == 3) ? (n - 1) : o.s[j];
+        P2[j] = sel3(sj, P[0], P[1], P[2], P[3]);
+        A2[j] = seli(sj, IA[0], IA[1], IA[2], IA[3]);
+        B2[j] = seli(sj, IB[0], IB[1], IB[2], IB[3]);
       }
-      for (int j = 0; j < nn; ++j) {
-        g.P[j] = P2[j];
-        g.ia[j] = a2[j];
-        g.ib[j] = b2[j];
-      }
-      g.n = nn;
     }
-    for (int j = 0; j < g.n; ++j) g.wmax2 = fmaxf(g.wmax2, dot(g.P[j], g.P[j]));
-    if (dot(v, v) <= contact * contact * g.wmax2) {
+    if (nn < 4) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        P[j] = P2[j];
+        IA[j] = A2[j];
+        IB[j] = B2[j];
+      }
+    }
+    n = nn;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j < n) wmax2 = fmaxf(wmax2, dot(P[j], P[j]));
+    if (dot(v, v) <= contact * contact * wmax2) {
       g.exit = GJK_EXIT_CONTACT;
       break;
     }
-    if (g.n == 4) {
+    if (n == 4) {
       g.exit = GJK_EXIT_ENCLOSED;
       break;
     }
@@ -629,8 +678,16 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
       break;
     }
   }
-  g.status |= g.exit << 16;
+  g.n = n;
+  g.wmax2 = wmax2;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    g.P[j] = P[j];
+    g.ia[j] = IA[j];
+    g.ib[j] = IB[j];
+  }
   if (k == cfg.gjk_max_iter && g.n != 4) g.status |= OGX_S_GJK_CAP;
+  g.status |= g.exit << 16;
   g.iters = k;
   g.v = v;
   g.dist = sqrtf(dot(v, v));
@@ -638,10 +695,12 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
   float lam[4];
   simplex_weights(g, lam);
   fv3 w0 = v3<float>(0.f, 0.f, 0.f), w1 = w0;
-  for (int j = 0; j < g.n; ++j) {
-    w0 = w0 + B.point(0, g.ia[j]) * lam[j];
-    w1 = w1 + B.point(1, g.ib[j]) * lam[j];
-  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    if (j < n) {
+      w0 = w0 + B.point(0, IA[j]) * lam[j];
+      w1 = w1 + B.point(1, IB[j]) * lam[j];
+    }
   g.w0 = w0;
   g.w1 = w1;
 
@@ -662,10 +721,11 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
     // more than twice the error of an FP32 support value against the exact value along
     // v64: FP32 dot rounding (4 eps amax |v|_1) plus the FP32 projection error of v
     // (16 eps |W| per component).
-    int exa[3] = {-1, -1, -1}, exb[3] = {-1, -1, -1};
-    for (int j = 0; j < g.n && j < 3; ++j) {
-      exa[j] = g.ia[j];
-      exb[j] = g.ib[j];
+    int exa[3], exb[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      exa[j] = j < n ? IA[j] : -1;
+      exb[j] = j < n ? IB[j] : -1;
     }
     float a1, ao, am, b1, bo, bm;
     B.scan_excl(t, 0, -v, exa, a1, ao, am);
@@ -689,8 +749,8 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
 // fl(x . d32) >= m - 2e with e >= |fl(x . d32) - x . d| <= 2 FLT_EPSILON |x|_max |d|_1
 // (rounding of d to FP32 plus the FP32 dot product), so only those few candidates are
 // evaluated in FP64.  Ties go to the lowest index.
-template <class Bodies>
-OGX_HD int exact_support(const Bodies& B, int w, dv3 d, double& val) {
+template <class Team, class Bodies>
+OGX_HD int exact_support(const Team& t, const Bodies& B, int w, dv3 d, double& val) {
   const MemBodies& M = B.mem_view();
   const fv3 fd = cvt<float>(d);
   const float* X = M.base[w];
@@ -698,22 +758,25 @@ OGX_HD int exact_support(const Bodies& B, int w, dv3 d, double& val) {
   const float* Z = Y + M.n4[w];
   const int n = M.n[w];
   float m = -INFINITY, amax = 0.0f;
-  for (int i = 0; i < n; ++i) {
+  for (int i = t.lane(); i < n; i += Team::L) {
     m = fmaxf(m, sdot(X[i], Y[i], Z[i], fd));
     amax = fmaxf(amax, fmaxf(fabsf(X[i]), fmaxf(fabsf(Y[i]), fabsf(Z[i]))));
   }
+  m = t.fmax_(m);
+  amax = t.fmax_(amax);
   const float e = 4.0f * FLT_EPSILON * amax * (fabsf(fd.x) + fabsf(fd.y) + fabsf(fd.z)) + FLT_MIN;
   const float lo = m - 2.0f * e;
   double best = -INFINITY;
-  int bi = 0;
-  for (int i = 0; i < n; ++i) {
+  int bi = 0x7fffffff;
+  for (int i = t.lane(); i < n; i += Team::L) {
     if (sdot(X[i], Y[i], Z[i], fd) < lo) continue;
     const double x = (double)X[i] * d.x + (double)Y[i] * d.y + (double)Z[i] * d.z;
-    if (x > best) {
+    if (x > best || (x == best && i < bi)) {
       best = x;
       bi = i;
     }
   }
+  t.argmax_d(best, bi);
   val = best;
   return bi;
 }
@@ -721,8 +784,8 @@ OGX_HD int exact_support(const Bodies& B, int w, dv3 d, double& val) {
 // FP64 continuation of GJK from the FP32 result: exact supports, FP64 sub-distance,
 // stop when the FP64 gap |v|^2 - v.w <= 1e-13 |v|^2 or the support repeats.  Certifies
 // (or corrects) the FP32 answer; sets g.n = 4 if the origin turns out to be enclosed.
-template <class Bodies>
-OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
+template <class Team, class Bodies>
+OGX_HD void gjk_refine(const Team& t, const Bodies& B, GjkState& g, int max_iter) {
   const bool certain = g.certain;
   Sx<double> s;
   int ia[4], ib[4];
@@ -770,8 +833,8 @@ OGX_HD void gjk_refine(const Bodies& B, GjkState& g, int max_iter) {
   if (certain) it = max_iter + 1;  // the FP32 pass proved the simplex final
   for (; it < max_iter; ++it) {
     double va, vb;
-    const int xa = exact_support(B, 0, -v, va);
-    const int xb = exact_support(B, 1, v, vb);
+    const int xa = exact_support(t, B, 0, -v, va);
+    const int xb = exact_support(t, B, 1, v, vb);
     const dv3 w = B.dpoint(0, xa) - B.dpoint(1, xb);
     const double vv = dot(v, v);
     // FP64 gap test.  In exact arithmetic v.p_j = |v|^2 for every vertex p_j of the

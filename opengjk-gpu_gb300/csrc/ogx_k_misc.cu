@@ -83,38 +83,68 @@ __global__ void k_bin(DevBatch B) {
   }
 }
 
-// FP64 continuation of GJK for the pairs whose FP32 distance is not certain (one thread
-// per pair: the FP64 units see full warps).  A pair found enclosed joins its bucket's
-// EPA list; the others get their normal from the refined witnesses.
+// After FP64 refinement: contacts join their bucket's EPA list, separated pairs get their
+// normal from the refined witnesses.
+__device__ void refine_store(const DevBatch& B, int p, const BodyRef& ra, const BodyRef& rb, const GjkState& g) {
+  store_simplex(B.smp + p, g);
+  B.dist[p] = g.dist;
+  if (B.status) B.status[p] |= g.status;
+  if (B.mode == kModeGjkEpa) {
+    if (gjk_contact(g)) {
+      const int bucket = bucket_of(ra.n > rb.n ? ra.n : rb.n);
+      const int e = atomicAdd(B.counts + kCntEpa + bucket, 1);
+      B.elists[(size_t)bucket * B.npairs + e] = p;
+    } else {
+      store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
+    }
+  }
+}
+
+// FP64 re-solve of separated pairs (one thread per pair: the FP64 units see full
+// warps).  Pairs whose final support the GJK kernel proved exact only need the exact
+// closest point of their simplex; the others are passed to k_refine_full.
 __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   const int cnt = B.counts[kCntRefine];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const RefineRec rr = B.refine[k];
+    if (!rr.certain) {
+      const int q = atomicAdd(B.counts + kCntRefineFull, 1);
+      B.refine_full[q] = rr.pair;
+      continue;
+    }
     const int p = rr.pair;
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
     MemBodies mb;
     mb.bind(B.pool, ra, rb);
-    gkSimplex* s = B.smp + p;
     GjkState g;
-    load_simplex(s, B.dist[p], g);
-    g.wa = rr.wa;
-    g.wb = rr.wb;
-    g.certain = rr.certain != 0;
-    gjk_refine(mb, g, kRefineIters);
-    store_simplex(s, g);
-    B.dist[p] = g.dist;
-    if (B.status) B.status[p] |= g.status;
-    const bool contact = gjk_contact(g);
-    if (B.mode == kModeGjkEpa) {
-      if (contact) {
-        const int bucket = bucket_of(ra.n > rb.n ? ra.n : rb.n);
-        const int e = atomicAdd(B.counts + kCntEpa + bucket, 1);
-        B.elists[(size_t)bucket * B.npairs + e] = p;
-      } else {
-        store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
-      }
-    }
+    load_simplex(B.smp + p, B.dist[p], g);
+    g.certain = true;
+    SerialTeam one;
+    gjk_refine(one, mb, g, kRefineIters);
+    refine_store(B, p, ra, rb, g);
+  }
+}
+
+// FP64 continuation of GJK for the pairs with an uncertain FP32 support: one warp per
+// pair, the exact-support scans split over the lanes.
+__global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
+  const WarpTeam<32> t;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int cnt = B.counts[kCntRefineFull];
+  for (int k = warp; k < cnt; k += nwarps) {
+    const int p = B.refine_full[k];
+    const int2 pr = B.pairs[p];
+    const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
+    MemBodies mb;
+    mb.bind(B.pool, ra, rb);
+    GjkState g;
+    load_simplex(B.smp + p, B.dist[p], g);
+    g.certain = false;
+    gjk_refine(t, mb, g, kRefineIters);
+    if (t.lane() == 0) refine_store(B, p, ra, rb, g);
+    __syncwarp();
   }
 }
 
@@ -169,8 +199,9 @@ cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_refine(const DevBatch& B, int grid, cudaStream_t st) {
+cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st) {
   k_refine<<<grid, 128, 0, st>>>(B);
+  k_refine_full<<<grid_full, 128, 0, st>>>(B);
   return cudaGetLastError();
 }
 

@@ -49,7 +49,8 @@ constexpr int kCntGjk = 0;                  // [0, kBuckets)
 constexpr int kCntEpa = kBuckets;           // [kBuckets, 2 kBuckets)
 constexpr int kCntPolish = 2 * kBuckets;    // EPA faces to re-solve in FP64
 constexpr int kCntRefine = 2 * kBuckets + 1;  // separated pairs to refine in FP64
-constexpr int kCntSlots = 2 * kBuckets + 2;
+constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to continue in FP64
+constexpr int kCntSlots = 2 * kBuckets + 3;
 constexpr int kRefineIters = 16;
 
 struct DevBatch {
@@ -67,6 +68,7 @@ struct DevBatch {
   int* counts;      // kCntSlots
   PolishRec* polish;
   RefineRec* refine;  // npairs entries
+  int* refine_full;   // npairs entries: pair ids whose FP32 support was not certain
   ogx_config cfg;
   int mode;
 };
@@ -256,7 +258,7 @@ int epa_variants_a(const KernelInfo** out);
 int epa_variants_b(const KernelInfo** out);
 
 // non-template kernels (ogx_k_misc.cu)
-cudaError_t launch_refine(const DevBatch& B, int grid, cudaStream_t st);
+cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st);
 cudaError_t refine_occupancy(int block, int* per_sm);
 cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st);

@@ -5,7 +5,10 @@ provider here); every computation is a call into libogx.so.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
+import sys
+import weakref
 
 import numpy as np
 
@@ -14,6 +17,26 @@ from ._lib import SIMPLEX_DTYPE, check
 
 MODE_GJK, MODE_GJK_EPA, MODE_EPA = 1, 2, 3
 
+# Engine objects still open at exit are closed by an atexit hook (pools before their
+# contexts), while the CUDA runtime and torch are still intact; objects that are
+# garbage-collected during interpreter shutdown are left to the process exit.
+_live_pools: "weakref.WeakSet" = weakref.WeakSet()
+_live_ctxs: "weakref.WeakSet" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    for p in list(_live_pools):
+        try:
+            p.close()
+        except Exception:
+            pass
+    for c in list(_live_ctxs):
+        try:
+            c.close()
+        except Exception:
+            pass
+
 
 def _torch():
     import torch
@@ -21,8 +44,9 @@ def _torch():
 
 
 class Context:
-    """One engine instance on one GPU, bound to a CUDA stream (default: torch's
-    current stream, so that engine calls order with torch work)."""
+    """One engine instance on one GPU, bound to a torch CUDA stream (default: a stream of
+    its own).  `run` orders the engine's work after the caller's current torch stream and
+    makes that stream wait for it, so results behave like any other torch op's."""
 
     def __init__(self, device: int = 0, config: _lib.Config | None = None, stream=None):
         torch = _torch()
@@ -31,20 +55,27 @@ class Context:
         self.lib = _lib.load()
         self.device = device
         torch.cuda.set_device(device)
-        if stream is None:
-            stream = torch.cuda.current_stream(device)
+        if stream is None or stream.cuda_stream == 0:
+            # the C API reads a NULL stream as "create one"; keep the stream visible here
+            stream = torch.cuda.Stream(device)
         self.stream = stream
         h = ctypes.c_void_p()
         cfgp = ctypes.byref(config) if config is not None else None
         check(self.lib.ogx_ctx_create(device, cfgp, ctypes.c_void_p(stream.cuda_stream), ctypes.byref(h)))
         self.handle = h
+        _live_ctxs.add(self)
 
     def close(self):
         if self.handle:
+            for p in list(_live_pools):  # a pool cannot outlive its context
+                if p.ctx is self:
+                    p.close()
             self.lib.ogx_ctx_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -105,11 +136,12 @@ class Context:
         return self.kernel_choice()
 
     def work_counts(self) -> dict:
-        c = (ctypes.c_int32 * 16)()
-        n = self.lib.ogx_ctx_work_counts(self.handle, c, 16)
-        if n != 16:
+        c = (ctypes.c_int32 * 17)()
+        n = self.lib.ogx_ctx_work_counts(self.handle, c, 17)
+        if n != 17:
             raise _lib.OgxError(-2, "work counts unavailable")
-        return {"gjk": list(c[0:7]), "epa": list(c[7:14]), "polish": int(c[14]), "refine": int(c[15])}
+        return {"gjk": list(c[0:7]), "epa": list(c[7:14]), "polish": int(c[14]), "refine": int(c[15]),
+                "refine_full": int(c[16])}
 
 
 class Pool:
@@ -122,6 +154,7 @@ class Pool:
         h = ctypes.c_void_p()
         check(ctx.lib.ogx_pool_create(ctx.handle, int(counts.shape[0]), counts.ctypes.data, ctypes.byref(h)))
         self.handle = h
+        _live_pools.add(self)
 
     @property
     def num_bodies(self) -> int:
@@ -155,11 +188,13 @@ class Pool:
         return pts.value, bodies.value
 
     def close(self):
-        if self.handle:
+        if self.handle and self.ctx.handle:
             self.ctx.lib.ogx_pool_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -195,6 +230,9 @@ def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Resu
     n = int(pairs_dev.shape[0])
     if out is None:
         out = Results(n, pairs_dev.device, with_normals=(mode != MODE_GJK))
+    cur = torch.cuda.current_stream(pairs_dev.device)
+    if cur != ctx.stream:
+        ctx.stream.wait_stream(cur)  # inputs and output buffers are ready
     P = ctypes.c_void_p
     args = [ctx.handle, pool.handle, n, P(pairs_dev.data_ptr()), P(out.simplex.data_ptr()), P(out.dist.data_ptr())]
     if mode == MODE_GJK:
@@ -205,6 +243,8 @@ def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Resu
         check(ctx.lib.ogx_epa(*args, P(out.normal.data_ptr()), P(out.status.data_ptr())))
     else:
         raise ValueError(mode)
+    if cur != ctx.stream:
+        cur.wait_stream(ctx.stream)  # later torch work sees the results
     return out
 
 

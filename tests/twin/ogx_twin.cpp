@@ -42,7 +42,7 @@ void one(const Job& J, int i, EpaMem& M) {
   // result, separated pairs are then re-solved in FP64, contacts go through EPA
   bool contact = gjk_contact(g);
   if (g.polish) {
-    gjk_refine(B, g, 16);
+    gjk_refine(t, B, g, 16);
     contact = gjk_contact(g);
   }
   gkSimplex& s = J.smp[i];
