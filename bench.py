@@ -78,29 +78,37 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.samples = []
-        self._stop = threading.Event()
+        self._proc = None
         self._t = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                r = subprocess.run(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                    "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if r.returncode == 0 and r.stdout.strip():
-                    self.samples.append([x.strip() for x in r.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._proc.stdout:
+            f = [x.strip() for x in line.strip().split(",")]
+            if len(f) >= 7:
+                self.samples.append(f)
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            # one nvidia-smi process sampling every 100 ms until stopped
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self._proc = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        if self._t:
-            self._t.join(timeout=10)
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+            if self._t:
+                self._t.join(timeout=5)
 
     def summary(self):
         if not self.samples:
@@ -136,6 +144,17 @@ def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
     return {"value": n / dt, "unit": "pairs/s", "cores": threads if not use_ref else threads,
             "kind": kind, "sample": f"first {n} pairs of the workload, FP32 reference tolerances, "
                                    f"{threads} threads, {dt:.1f} s"}
+
+
+def load_traffic() -> dict:
+    """DRAM bytes per work unit of each kernel, from the committed ncu summary
+    (profiles/dram_traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one
+    captured launch divided by the units it processed)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
 
 
 def _cpu_run(orc, b, mode, threads, use_ref):
@@ -224,6 +243,7 @@ def run_ours(args):
     ktimes = ctx.kernel_times()
     counts = ctx.work_counts()
     ctx.set_timing(False)
+    dist_after = out.dist.cpu().numpy()
     if args.profile_launches:
         torch.cuda.synchronize()
         return
@@ -303,30 +323,34 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     tot = sum(t for _, t in ktimes)
-    dom_name, dom_ms = max(ktimes, key=lambda kv: kv[1])
-    from ogx.workloads import Batch  # noqa: F401
+    # kernel families: the seven bucket launches of k_gjk (and of k_epa) are one kernel
+    fam_ms, fam_n = {}, {}
+    for name, t in ktimes:
+        f = "k_" + name.split("<")[0].split(">")[0]
+        fam_ms[f] = fam_ms.get(f, 0.0) + t
+        fam_n[f] = fam_n.get(f, 0) + 1
+    dom = max(fam_ms, key=fam_ms.get)
     nv = batch.pair_vertex_counts()
-    m = np.maximum(batch.counts[batch.pairs[:, 0]], batch.counts[batch.pairs[:, 1]])
-    edges = [0, 16, 32, 64, 128, 256, 512, 1 << 30]
-    bucket = np.searchsorted(edges, m, side="left") - 1
-    kind, lab = dom_name.split("<=")[0].split(">")[0], dom_name
-    bi = ["<=16", "<=32", "<=64", "<=128", "<=256", "<=512", ">512"]
-    b_id = [i for i, s in enumerate(bi) if dom_name.endswith(s)]
-    if b_id and kind == "gjk":
-        sel = bucket == b_id[0]
-        dom_bytes = int(12 * nv[sel].sum() + 120 * sel.sum())
-    elif b_id and kind == "epa":
-        # contacts of the bucket: their points plus the EPA outputs (depth, witnesses, normal)
-        frac = counts["epa"][b_id[0]] / max(1, counts["gjk"][b_id[0]])
-        sel = bucket == b_id[0]
-        dom_bytes = int(frac * (12 * nv[sel].sum() + 8 * sel.sum()) + 40 * counts["epa"][b_id[0]])
+    contact = dist_after <= 0.0
+    if dom == "k_gjk":
+        # every pair: both bodies' points, the pair, distance and simplex
+        dom_bytes, units = int(12 * nv.sum() + 120 * n), n
+    elif dom == "k_epa":
+        # every contact: both bodies' points, the pair, depth, simplex and normal
+        dom_bytes, units = int(12 * nv[contact].sum() + 132 * contact.sum()), int(contact.sum())
     else:
-        dom_bytes = int(alg_bytes)
-    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+        dom_bytes, units = int(alg_bytes), n
+    achieved = dom_bytes / (fam_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tr = load_traffic().get(dom)
+    if tr and units:
+        traffic = tr["bytes_per_unit"] * units / fam_n[dom]
     pipeline_gbs = alg_bytes / (ms / 1e3) / 1e9
-    roof = {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
-            "kernel_share": dom_ms / tot if tot else None,
+    roof = {"bound": "hbm", "kernel": f"{dom} ({fam_n[dom]} bucket launches)", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+            "traffic": traffic, "traffic_source": tr["source"] if tr else None,
+            "algorithmic_bytes_per_launch": dom_bytes / fam_n[dom], "units_per_step": units,
+            "kernel_share": fam_ms[dom] / tot if tot else None,
             "pipeline_achieved": pipeline_gbs, "pipeline_frac": pipeline_gbs / peak,
             "algorithmic_bytes_per_step": int(alg_bytes)}
 
