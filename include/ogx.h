@@ -155,6 +155,23 @@ ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lan
 ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                         const gkCollisionPair* d_pairs, int reps);
 
+/* GJK then EPA that allocates no device memory.  No counterpart in the reference.
+ * For callers that must not allocate device memory at query time: loops whose device
+ * memory belongs to their own arena, real-time ticks that cannot take allocator
+ * latency, plugins whose host forbids them to allocate.  The pool is given by
+ * its device arrays in the engine layout (ogx_pool_device_layout, or written by the
+ * caller); the caller passes the pairs and all outputs.  The pipeline's work lists live
+ * in one static device array of 1,769,728 bytes that every GPU loading this library
+ * holds until exit.  At most 16384 pairs per call (OGX_ERR_CAPACITY beyond).  Each call
+ * clears the array's counters itself; nothing has to be zeroed by the caller.  All calls
+ * share the array, so calls that overlap on the GPU race: serialise them.  The first call on
+ * a device looks up the array's address and the launch sizes -- make it before any
+ * stream capture.  cfg NULL = defaults; stream = cudaStream_t (NULL: legacy stream). */
+ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_bodies, int num_bodies,
+                               int npairs, const gkCollisionPair* d_pairs,
+                               gkSimplex* d_simplices, float* d_distances, float* d_normals,
+                               int32_t* d_status, const ogx_config* cfg, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Reference-compatible entry points.  Same arguments, meaning and output     */
 /* conventions as OpenGJK-GPU's host API; each call returns when its results  */
