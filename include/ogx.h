@@ -137,8 +137,9 @@ ogx_status ogx_ctx_set_timing(ogx_ctx* ctx, int on);
 int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
 /* Work counts of the last call (waits for it): pairs per GJK bucket [0, 7), contacts
  * per EPA bucket [7, 14), EPA faces re-solved in FP64 [14], pairs whose GJK result was
- * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16].
- * cap must be >= 17. */
+ * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16],
+ * contacts whose EPA outgrew the bucket kernels' working set and ran again at full
+ * capacity [17].  cap must be >= 18. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 /* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most
@@ -161,7 +162,7 @@ ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
  * latency, plugins whose host forbids them to allocate.  The pool is given by
  * its device arrays in the engine layout (ogx_pool_device_layout, or written by the
  * caller); the caller passes the pairs and all outputs.  The pipeline's work lists live
- * in one static device array of 1,769,728 bytes that every GPU loading this library
+ * in one static device array of 1,835,264 bytes that every GPU loading this library
  * holds until exit.  At most 16384 pairs per call (OGX_ERR_CAPACITY beyond).  Each call
  * clears the array's counters itself; nothing has to be zeroed by the caller.  All calls
  * share the array, so calls that overlap on the GPU race: serialise them.  The first call on

@@ -177,6 +177,14 @@ OGX_HD Config reference_config() {
   return c;
 }
 
+OGX_HD int popc32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __popc(x);
+#else
+  return __builtin_popcount(x);
+#endif
+}
+
 // EPA capacities.  With at most 64 expansions the polytope has at most 68 vertices and
 // (Euler, closed triangulated surface) 2*68-4 = 132 faces.
 constexpr int kEpaVmax = 68;
@@ -194,6 +202,8 @@ struct SerialTeam {
   OGX_HD void argmax2(float&, int&, float&) const {}
   OGX_HD void argmax_d(double&, int&) const {}
   OGX_HD bool any(bool p) const { return p; }
+  OGX_HD uint32_t ballot(bool p) const { return p ? 1u : 0u; }
+  OGX_HD uint32_t below() const { return 0u; }
   OGX_HD int excl_scan(int x, int& total) const {
     total = x;
     return 0;
@@ -269,6 +279,13 @@ struct WarpTeam {
     }
   }
   __device__ bool any(bool p) const { return (__ballot_sync(mask, p) & mask) != 0u; }
+  // bit l = predicate of team lane l
+  __device__ uint32_t ballot(bool p) const {
+    const uint32_t b = __ballot_sync(mask, p);
+    return L == 32 ? b : (b >> ((threadIdx.x & 31) & ~(L - 1))) & ((1u << L) - 1u);
+  }
+  // team lanes below this one
+  __device__ uint32_t below() const { return (1u << ln) - 1u; }
   __device__ int excl_scan(int x, int& total) const {
     int inc = x;
 #pragma unroll

@@ -101,7 +101,7 @@ constexpr int kBucketCap[kBuckets] = {16, 32, 64, 128, 256, 512, 0};
 
 std::mutex g_init_mu;
 int g_init_device = -1;
-int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0;
+int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0, g_grid_spill = 0;
 // per-device autotuned choices (variant index per bucket), -1 = not tuned
 int g_tuned[16][2][kBuckets];
 bool g_tuned_valid[16];
@@ -130,7 +130,7 @@ int default_choice(const std::vector<Launch>& vs, int b) {
 }
 
 ogx_status init_variant(Launch* k, bool epa, int sms) {
-  k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMem) : 0;
+  k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMemSmall) : 0;
   cudaError_t e;
   if (k->smem > 48 * 1024) {
     e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -158,6 +158,8 @@ ogx_status init_kernels(int device) {
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = gjk_variants_b(&t);
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = gjk_variants_c(&t);
+  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_a(&t);
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_b(&t);
@@ -176,6 +178,9 @@ ogx_status init_kernels(int device) {
   e = polish_occupancy(kBlock, &per_sm);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy(k_polish)");
   g_grid_polish = std::max(1, per_sm) * sms;
+  e = epa_spill_occupancy(kBlock, &per_sm);
+  if (e != cudaSuccess) return e;
+  g_grid_spill = std::max(1, per_sm) * sms;
   e = refine_occupancy(kBlock, &per_sm);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy(k_refine)");
   g_grid_refine = std::max(1, per_sm) * sms;
@@ -251,6 +256,8 @@ void ogx_ctx::free_scratch() {
   cudaFree(d_counts);
   cudaFree(d_refine);
   cudaFree(d_refine_full);
+  cudaFree(d_spill);
+  d_spill = nullptr;
   d_refine = nullptr;
   d_refine_full = nullptr;
   d_lists = d_elists = d_counts = nullptr;
@@ -359,6 +366,7 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
       (e = cudaMalloc(&d_polish, cap * sizeof(PolishRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine, cap * sizeof(RefineRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine_full, cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_spill, cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_counts, 64 * sizeof(int))) != cudaSuccess) {
     free_scratch();
     return ogx_cuda_fail(e, "scratch allocation");
@@ -515,7 +523,7 @@ extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* co
 
 ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, int nbodies,
                    int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
-                   float* d_nrm, int32_t* d_status, int mode) {
+                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm) {
   if (npairs < 0) return ogx_fail(OGX_ERR_INVALID, "npairs < 0");
   if (npairs == 0) {
     ctx->last_launches = 0;
@@ -542,6 +550,8 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.polish = ctx->d_polish;
   B.refine = ctx->d_refine;
   B.refine_full = ctx->d_refine_full;
+  B.spill = ctx->d_spill;
+  B.warm = d_warm;
   B.cfg = ctx->cfg;
   B.mode = mode;
   cudaStream_t st = ctx->stream;
@@ -579,6 +589,11 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
       k.fn<<<k.grid, kBlock, k.smem, st>>>(B, b);
       ++launches;
     }
+    // contacts that outgrew the bucket kernels' working set, at full capacity
+    ctx->mark("epa_spill");
+    e = launch_epa_spill(B, g_grid_spill, st);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
+    ++launches;
   }
   if (mode != kModeGjk && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("polish");

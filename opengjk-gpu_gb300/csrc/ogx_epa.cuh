@@ -29,19 +29,28 @@
 
 namespace ogx {
 
-// Shared-memory working set of one pair (5728 bytes).
-struct EpaMem {
-  float4 fn[kEpaFmax];          // unit outward normal, w = plane distance from origin
-  float4 vp[kEpaVmax];          // polytope vertices (Minkowski points)
-  int2 vid[kEpaVmax];           // (index in body 1, index in body 2)
-  uint8_t fv[kEpaFmax][4];      // face vertices a, b, c; [3] = 1 when the face is alive
-  uint8_t fa[kEpaFmax][4];      // fa[f][e]: face across edge e = (v_e, v_{e+1 mod 3})
-  uint8_t vis[kEpaFmax];        // visible from the new point (this step)
-  uint8_t freel[kEpaFmax];      // free face slots (this step)
-  uint8_t hz[kEpaFmax][4];      // horizon edges (this step): a, b, face beyond
-  uint8_t hstart[kEpaVmax];     // new face whose horizon edge starts at vertex
-  uint8_t hend[kEpaVmax];       // new face whose horizon edge ends at vertex
+// Shared-memory working set of one pair, for at most VMAX polytope vertices and FMAX
+// faces (5728 bytes at 68 / 132, the capacity of 64 expansions; 2288 bytes at 28 / 52).
+template <int VMAX, int FMAX>
+struct EpaMemT {
+  static constexpr int kV = VMAX;
+  static constexpr int kF = FMAX;
+  float4 fn[FMAX];          // unit outward normal, w = plane distance from origin
+  float4 vp[VMAX];          // polytope vertices (Minkowski points)
+  int2 vid[VMAX];           // (index in body 1, index in body 2)
+  uint8_t fv[FMAX][4];      // face vertices a, b, c; [3] = 1 when the face is alive
+  uint8_t fa[FMAX][4];      // fa[f][e]: face across edge e = (v_e, v_{e+1 mod 3})
+  uint8_t vis[FMAX];        // visible from the new point (this step)
+  uint8_t vlist[FMAX];      // visible faces in increasing order (this step)
+  uint8_t hz[FMAX][4];      // horizon edges (this step): a, b, face beyond
+  uint8_t hstart[VMAX];     // new face whose horizon edge starts at vertex
+  uint8_t hend[VMAX];       // new face whose horizon edge ends at vertex
 };
+// full capacity: every pair within the 64-expansion cap
+typedef EpaMemT<kEpaVmax, kEpaFmax> EpaMem;
+// small capacity: 24 expansions; a pair that needs more is handed to a full-capacity pass
+constexpr int kEpaSmallIters = 24;
+typedef EpaMemT<4 + kEpaSmallIters, 4 + 2 * kEpaSmallIters> EpaMemSmall;
 
 struct EpaOut {
   float dist;   // -depth for contacts, the GJK distance otherwise
@@ -51,6 +60,7 @@ struct EpaOut {
   int iters;
   int face[3][2];  // vertex index pairs of the final face (FP64 re-solve)
   bool polish;
+  bool spill;      // ran out of (small) capacity: nothing written, run again at full capacity
 };
 
 OGX_HD fv3 unit_or_x(fv3 d) {
@@ -71,8 +81,8 @@ OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
 }
 
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
-template <class Bodies>
-OGX_HD float4 face_plane(const EpaMem& M, const Bodies& B, int a, int b, int c, bool escalate,
+template <class Mem, class Bodies>
+OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, bool escalate,
                          int& status) {
   const float4 P0 = M.vp[a], P1 = M.vp[b], P2 = M.vp[c];
   const fv3 p0 = v3<float>(P0.x, P0.y, P0.z);
@@ -163,8 +173,8 @@ OGX_HD int tri_weights(fv3 p0, fv3 p1, fv3 p2, float* l) {
 // that edge lies in the same plane (the Minkowski face of an edge-edge or face-face
 // contact is split into coplanar triangles), the neighbour that holds the projection is
 // used, so that w0 - w1 = depth * normal holds.
-template <class Bodies>
-OGX_HD void epa_emit(const EpaMem& M, const Bodies& B, int f, float tie, EpaOut& o) {
+template <class Mem, class Bodies>
+OGX_HD void epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o) {
   int a = M.fv[f][0], b = M.fv[f][1], c = M.fv[f][2];
   float l[3];
   for (int hop = 0; hop < 4; ++hop) {
@@ -261,15 +271,28 @@ OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
 }
 
 // Run EPA for one pair whose GJK result is g.  `M` is this pair's shared working set.
-template <class Team, class Bodies>
+//
+// One expansion step, with the faces of the polytope split over the team's lanes
+// (face f on lane f mod L):
+//   1. every lane tests its live faces for visibility from the new point q and keeps the
+//      closest face that stays (not visible);
+//   2. visible faces are ranked in increasing slot order and horizon edges in increasing
+//      (face, edge) order with ballots, so slot assignment does not depend on L; new face
+//      k takes the k-th visible slot, then fresh slots at the end of the used range;
+//   3. faces beyond the horizon are relinked to the new faces, the visible faces retired;
+//   4. new faces are linked to each other through the per-vertex tables and their planes
+//      computed; the closest new face joins the lane's candidate.
+// The next step's closest face is the team's minimum over the candidates.
+template <class Team, class Bodies, class Mem>
 OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const GjkState& g,
-                     EpaMem& M, EpaOut& o) {
+                     Mem& M, EpaOut& o, bool can_spill) {
   const int L = Team::L;
   const int lane = t.lane();
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
   o.status = 0;
   o.iters = 0;
   o.polish = false;
+  o.spill = false;
   o.dist = g.dist;
   o.w0 = g.w0;
   o.w1 = g.w1;
@@ -278,21 +301,35 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   o.status |= OGX_S_EPA_RUN;
 
   // ---- grow the simplex to a tetrahedron (EPA.c:375-583)
+  // simplex in registers: every index below is a constant after unrolling
   fv3 P[4];
   int IA[4], IB[4];
   int n = g.n;
-  for (int j = 0; j < n; ++j) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
     P[j] = g.P[j];
     IA[j] = g.ia[j];
     IB[j] = g.ib[j];
   }
   const float e2 = FLT_EPSILON * FLT_EPSILON;
   auto is_new = [&](fv3 q, int qa, int qb) {
-    for (int j = 0; j < n; ++j) {
+    bool fresh = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
       const fv3 d = q - P[j];
-      if (dot(d, d) < e2 || (IA[j] == qa && IB[j] == qb)) return false;
+      if (j < n && (dot(d, d) < e2 || (IA[j] == qa && IB[j] == qb))) fresh = false;
     }
-    return true;
+    return fresh;
+  };
+  auto append = [&](fv3 q, int qa, int qb) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j == n) {
+        P[j] = q;
+        IA[j] = qa;
+        IB[j] = qb;
+      }
+    ++n;
   };
   if (n == 1) {
     int qa, qb;
@@ -301,7 +338,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       epa_touch(B.point(0, qa), B.point(1, qb), o);
       return;
     }
-    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+    append(q, qa, qb);
   }
   if (n == 2) {
     const fv3 e = P[1] - P[0];
@@ -316,7 +353,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       epa_touch(B.point(0, qa), B.point(1, qb), o);
       return;
     }
-    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+    append(q, qa, qb);
   }
   if (n == 3) {
     fv3 d = cross(P[1] - P[0], P[2] - P[0]);
@@ -329,35 +366,49 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
         return;
       }
     }
-    P[n] = q; IA[n] = qa; IB[n] = qb; ++n;
+    append(q, qa, qb);
   }
 
   // ---- tetrahedron
   const float vol = dot(P[1] - P[0], cross(P[2] - P[0], P[3] - P[0]));
-  // outward faces of a positively oriented tetrahedron (0,1,2,3); swap 1 and 2 otherwise
+  // outward faces of a positively oriented tetrahedron (0,1,2,3); swap 1 and 2 otherwise:
+  // (0, i2, i1), (0, i1, 3), (i1, i2, 3), (i2, 0, 3).  Face across edge k of face f
+  // (edge k = vertices k, k+1 mod 3) is the same for both orientations.
   const int i1 = vol >= 0.0f ? 1 : 2, i2 = vol >= 0.0f ? 2 : 1;
-  const int tri[4][3] = {{0, i2, i1}, {0, i1, 3}, {i1, i2, 3}, {i2, 0, 3}};
   float scale2 = 0.0f;
-  for (int j = lane; j < 4; j += L) {
-    M.vp[j] = make_float4_(P[j].x, P[j].y, P[j].z, 0.0f);
-    M.vid[j] = make_int2_(IA[j], IB[j]);
-  }
-  for (int j = 0; j < 4; ++j) scale2 = fmaxf(scale2, dot(P[j], P[j]));
-  for (int f = lane; f < kEpaFmax; f += L) M.fv[f][3] = 0;
-  t.sync();
-  for (int f = lane; f < 4; f += L) {
-    for (int k = 0; k < 3; ++k) M.fv[f][k] = (uint8_t)tri[f][k];
-    M.fv[f][3] = 1;
-    for (int k = 0; k < 3; ++k) {
-      const int a = tri[f][k], b = tri[f][(k + 1) % 3];
-      for (int h = 0; h < 4; ++h)
-        for (int m = 0; m < 3; ++m)
-          if (tri[h][m] == b && tri[h][(m + 1) % 3] == a) M.fa[f][k] = (uint8_t)h;
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      M.vp[j] = make_float4_(P[j].x, P[j].y, P[j].z, 0.0f);
+      M.vid[j] = make_int2_(IA[j], IB[j]);
     }
   }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) scale2 = fmaxf(scale2, dot(P[j], P[j]));
   t.sync();
   int st = 0;
-  for (int f = lane; f < 4; f += L) M.fn[f] = face_plane(M, B, M.fv[f][0], M.fv[f][1], M.fv[f][2], escalate, st);
+  // per-lane closest candidate (slot, plane distance); -1 = none
+  float cbd = INFINITY;
+  int cbest = -1;
+  for (int f = lane; f < 4; f += L) {
+    const int va = f == 2 ? i1 : (f == 3 ? i2 : 0);
+    const int vb = f == 0 ? i2 : (f == 1 ? i1 : (f == 2 ? i2 : 0));
+    const int vc = f == 0 ? i1 : 3;
+    M.fv[f][0] = (uint8_t)va;
+    M.fv[f][1] = (uint8_t)vb;
+    M.fv[f][2] = (uint8_t)vc;
+    M.fv[f][3] = 1;
+    // {3,2,1}, {0,2,3}, {0,3,1}, {0,1,2}
+    M.fa[f][0] = (uint8_t)(f == 0 ? 3 : 0);
+    M.fa[f][1] = (uint8_t)(f == 0 || f == 1 ? 2 : (f == 2 ? 3 : 1));
+    M.fa[f][2] = (uint8_t)(f == 0 ? 1 : (f == 1 ? 3 : (f == 2 ? 1 : 2)));
+    const float4 pl = face_plane(M, B, va, vb, vc, escalate, st);
+    M.fn[f] = pl;
+    if (pl.w < cbd) {
+      cbd = pl.w;
+      cbest = f;
+    }
+  }
   int nv = 4, fend = 4;
   t.sync();
 
@@ -368,16 +419,8 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   while (it < cfg.epa_max_iter) {
     ++it;
     // closest live face
-    float bd = INFINITY;
-    best = -1;
-    for (int f = lane; f < fend; f += L) {
-      if (!M.fv[f][3]) continue;
-      const float d = M.fn[f].w;
-      if (d < bd) {
-        bd = d;
-        best = f;
-      }
-    }
+    float bd = cbd;
+    best = cbest;
     t.argmin(bd, best);
     if (best < 0 || !(bd < INFINITY)) {
       o.status |= OGX_S_EPA_TOPOLOGY;
@@ -407,7 +450,11 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       done = true;
       break;
     }
-    if (nv >= kEpaVmax) {
+    if (nv >= Mem::kV) {
+      if (can_spill) {
+        o.spill = true;
+        return;
+      }
       o.status |= OGX_S_EPA_CAPACITY;
       done = true;
       break;
@@ -421,14 +468,25 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     scale2 = fmaxf(scale2, dot(q, q));
     const float vis_eps = cfg.epa_vis * scale;
 
-    // faces seen from q
-    for (int f = lane; f < fend; f += L) {
+    // 1. faces seen from q; the closest face that stays
+    cbd = INFINITY;
+    cbest = -1;
+    int nvis = 0;
+    for (int f0 = 0; f0 < fend; f0 += L) {
+      const int f = f0 + lane;
       bool s = false;
-      if (M.fv[f][3]) {
+      if (f < fend && M.fv[f][3]) {
         const float4 fp = M.fn[f];
         s = (fp.x * q.x + fp.y * q.y + fp.z * q.z) - fp.w > vis_eps;
+        if (!s && fp.w < cbd) {
+          cbd = fp.w;
+          cbest = f;
+        }
       }
-      M.vis[f] = s;
+      if (f < fend) M.vis[f] = s;
+      const uint32_t m = t.ballot(s);
+      if (s) M.vlist[nvis + popc32(m & t.below())] = (uint8_t)f;
+      nvis += popc32(m);
     }
     t.sync();
     // the closest face must be seen (gain >= tol > vis threshold); otherwise stop
@@ -437,60 +495,63 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       done = true;
       break;
     }
-    // horizon edges (edge e of a visible face whose neighbour is not visible) and free
-    // face slots, compacted over the lanes into hz[] and freel[]
-    int hcount = 0;
-    for (int f = lane; f < fend; f += L) {
-      if (!M.vis[f]) continue;
-      for (int e = 0; e < 3; ++e) hcount += M.vis[M.fa[f][e]] ? 0 : 1;
+    // 2. horizon edges: edge e of a visible face whose neighbour is not visible
+    int htot = 0;
+    for (int k0 = 0; k0 < nvis; k0 += L) {
+      const int k = k0 + lane;
+      bool h[3] = {false, false, false};
+      int f = 0;
+      if (k < nvis) {
+        f = M.vlist[k];
+        for (int e = 0; e < 3; ++e) h[e] = !M.vis[M.fa[f][e]];
+      }
+      const uint32_t m0 = t.ballot(h[0]), m1 = t.ballot(h[1]), m2 = t.ballot(h[2]);
+      const uint32_t lo = t.below();
+      int r = htot + popc32(m0 & lo) + popc32(m1 & lo) + popc32(m2 & lo);
+      for (int e = 0; e < 3; ++e) {
+        if (!h[e]) continue;
+        if (r < Mem::kF) {
+          M.hz[r][0] = M.fv[f][e];
+          M.hz[r][1] = M.fv[f][(e + 1) % 3];
+          M.hz[r][2] = M.fa[f][e];
+        }
+        ++r;
+      }
+      htot += popc32(m0) + popc32(m1) + popc32(m2);
     }
-    int fcount = 0;
-    for (int f = lane; f < kEpaFmax; f += L)
-      fcount += (f >= fend || !M.fv[f][3] || M.vis[f]) ? 1 : 0;
-    int htot, ftot;
-    const int hbase = t.excl_scan(hcount, htot);
-    const int fbase = t.excl_scan(fcount, ftot);
-    if (htot > ftot || htot < 3) {
-      o.status |= (htot > ftot) ? OGX_S_EPA_CAPACITY : OGX_S_EPA_TOPOLOGY;
+    // new face k goes to vlist[k] (k < nvis), else to fresh slot fend + k - nvis
+    if (htot < 3) {
+      o.status |= OGX_S_EPA_TOPOLOGY;
       done = true;
       break;
     }
-    {
-      int k = fbase;
-      for (int f = lane; f < kEpaFmax; f += L)
-        if (f >= fend || !M.fv[f][3] || M.vis[f]) M.freel[k++] = (uint8_t)f;
-      k = hbase;
-      for (int f = lane; f < fend; f += L) {
-        if (!M.vis[f]) continue;
-        for (int e = 0; e < 3; ++e) {
-          const int g2 = M.fa[f][e];
-          if (M.vis[g2]) continue;
-          M.hz[k][0] = M.fv[f][e];
-          M.hz[k][1] = M.fv[f][(e + 1) % 3];
-          M.hz[k][2] = (uint8_t)g2;
-          ++k;
-        }
+    if (fend + (htot > nvis ? htot - nvis : 0) > Mem::kF) {
+      if (can_spill) {
+        o.spill = true;
+        return;
       }
+      o.status |= OGX_S_EPA_CAPACITY;
+      done = true;
+      break;
     }
     t.sync();
-    // relink the faces outside the horizon, index the horizon by its vertices, retire
+    // 3. relink the faces outside the horizon, index the horizon by its vertices, retire
     // the visible faces
     for (int k = lane; k < htot; k += L) {
-      const int s = M.freel[k];
+      const int s = k < nvis ? M.vlist[k] : fend + k - nvis;
       const int a = M.hz[k][0], b = M.hz[k][1], g2 = M.hz[k][2];
       for (int m = 0; m < 3; ++m)
         if (M.fv[g2][m] == b && M.fv[g2][(m + 1) % 3] == a) M.fa[g2][m] = (uint8_t)s;
       M.hstart[a] = (uint8_t)s;
       M.hend[b] = (uint8_t)s;
     }
-    for (int f = lane; f < fend; f += L)
-      if (M.vis[f]) M.fv[f][3] = 0;
+    for (int k = lane; k < nvis; k += L) M.fv[M.vlist[k]][3] = 0;
     t.sync();
     // a vertex that starts (or ends) two horizon edges means the horizon is not one
     // simple loop; keep the closest face found this step and stop
     bool bad = false;
     for (int k = lane; k < htot; k += L) {
-      const int s = M.freel[k];
+      const int s = k < nvis ? M.vlist[k] : fend + k - nvis;
       bad |= (M.hstart[M.hz[k][0]] != s) || (M.hend[M.hz[k][1]] != s);
     }
     if (t.any(bad)) {
@@ -498,10 +559,9 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       done = true;
       break;
     }
-    // new face (a, b, p) across each horizon edge a->b
-    int my_new_max = -1;
+    // 4. new face (a, b, p) across each horizon edge a->b
     for (int k = lane; k < htot; k += L) {
-      const int s = M.freel[k];
+      const int s = k < nvis ? M.vlist[k] : fend + k - nvis;
       const int a = M.hz[k][0], b = M.hz[k][1];
       M.fv[s][0] = (uint8_t)a;
       M.fv[s][1] = (uint8_t)b;
@@ -509,27 +569,23 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       M.fa[s][0] = M.hz[k][2];
       M.fa[s][1] = M.hstart[b];
       M.fa[s][2] = M.hend[a];
-      M.fn[s] = face_plane(M, B, a, b, p, escalate, st);
+      const float4 pl = face_plane(M, B, a, b, p, escalate, st);
+      M.fn[s] = pl;
       M.fv[s][3] = 1;
-      my_new_max = my_new_max > s ? my_new_max : s;
+      if (pl.w < cbd || (pl.w == cbd && s < cbest)) {
+        cbd = pl.w;
+        cbest = s;
+      }
     }
-    const int new_max = t.imax(my_new_max);
-    fend = fend > new_max + 1 ? fend : new_max + 1;
+    if (htot > nvis) fend += htot - nvis;
     t.sync();
   }
   o.iters = it;
   o.status |= st ? OGX_S_EPA_ESCALATED : 0;
   if (!done) {
     // iteration cap: closest current face
-    float bd = INFINITY;
-    best = -1;
-    for (int f = lane; f < fend; f += L) {
-      if (!M.fv[f][3]) continue;
-      if (M.fn[f].w < bd) {
-        bd = M.fn[f].w;
-        best = f;
-      }
-    }
+    float bd = cbd;
+    best = cbest;
     t.argmin(bd, best);
     o.status |= OGX_S_EPA_CAP;
   }

@@ -525,24 +525,29 @@ OGX_HD int escalate_step(const MemBodies B, int n, const int* ia, const int* ib,
 }
 
 template <class Team, class Bodies>
-OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g) {
+OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g, int start_a = 0,
+                     int start_b = 0) {
   const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
-  const fv3 a0 = B.point(0, 0), b0 = B.point(1, 0);
+  // first point of the Minkowski difference: point 0 of each body (the reference's
+  // start), or a warm-start pair of vertex indices (e.g. the previous frame's simplex)
+  const int ia0 = start_a, ib0 = start_b;
+  const fv3 a0 = B.point(0, ia0), b0 = B.point(1, ib0);
   fv3 v = a0 - b0;
   // simplex in registers: slots 0..3, newest last; every index below is unrolled
   fv3 P[4];
   int IA[4], IB[4];
   P[0] = v;
   P[1] = P[2] = P[3] = v;
-  IA[0] = IB[0] = 0;
+  IA[0] = ia0;
+  IB[0] = ib0;
   IA[1] = IA[2] = IA[3] = IB[1] = IB[2] = IB[3] = -1;
   int n = 1;
   g.status = 0;
   g.exit = 0;
   float wmax2 = 0.0f;
   fv3 sa = a0, sb = b0;
-  int ia = 0, ib = 0;
+  int ia = ia0, ib = ib0;
   const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
   // |v| this small against the simplex points is below FP32 resolution: stop
   const float contact = reftol ? cfg.gjk_eps_tot : 0.5f * FLT_EPSILON;

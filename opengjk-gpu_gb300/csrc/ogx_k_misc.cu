@@ -194,6 +194,32 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// EPA at full capacity (EpaMem) over the spill list: one warp per contact, points read
+// from memory (any body size)
+__global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  EpaMem* mem = reinterpret_cast<EpaMem*>(smem_raw);
+  const WarpTeam<32> t;
+  EpaMem& M = mem[threadIdx.x / 32];
+  const int team = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  const int nteams = (gridDim.x * blockDim.x) / 32;
+  const int cnt = B.counts[kCntSpill];
+  for (int j = team; j < cnt; j += nteams) {
+    epa_item<32, 0>(t, B, B.spill[j], M, false);
+    t.sync();
+  }
+}
+
+cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st) {
+  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMem), st>>>(B);
+  return cudaGetLastError();
+}
+
+cudaError_t epa_spill_occupancy(int block, int* per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_epa_spill, block,
+                                                       (block / 32) * sizeof(EpaMem));
+}
+
 cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
   k_polish<<<grid, 128, 0, st>>>(B);
   return cudaGetLastError();

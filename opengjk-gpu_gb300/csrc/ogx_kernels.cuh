@@ -50,7 +50,8 @@ constexpr int kCntEpa = kBuckets;           // [kBuckets, 2 kBuckets)
 constexpr int kCntPolish = 2 * kBuckets;    // EPA faces to re-solve in FP64
 constexpr int kCntRefine = 2 * kBuckets + 1;  // separated pairs to refine in FP64
 constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to continue in FP64
-constexpr int kCntSlots = 2 * kBuckets + 3;
+constexpr int kCntSpill = 2 * kBuckets + 3;  // contacts that outgrew the small EPA capacity
+constexpr int kCntSlots = 2 * kBuckets + 4;
 constexpr int kRefineIters = 16;
 
 struct DevBatch {
@@ -69,6 +70,8 @@ struct DevBatch {
   PolishRec* polish;
   RefineRec* refine;  // npairs entries
   int* refine_full;   // npairs entries: pair ids whose FP32 support was not certain
+  int* spill;         // npairs entries: contacts to re-run at full EPA capacity
+  const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
   ogx_config cfg;
   int mode;
 };
@@ -160,10 +163,16 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
     const int2 pr = B.pairs[p];
+    const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
     typename SrcOf<L, K>::type src;
-    bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
+    bind_src<L>(src, B.pool, ra, rb, t.lane());
+    int2 ws = make_int2(0, 0);
+    if (B.warm) {
+      ws = B.warm[p];
+      if (ws.x < 0 || ws.x >= ra.n || ws.y < 0 || ws.y >= rb.n) ws = make_int2(0, 0);
+    }
     GjkState g;
-    gjk_pair(t, src, B.cfg, g);
+    gjk_pair(t, src, B.cfg, g, ws.x, ws.y);
     const bool contact = gjk_contact(g);
     const bool lead = t.lane() == 0;
     if (lead) {
@@ -189,49 +198,65 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
   }
 }
 
+// EPA of contact p by one team; returns false when the pair outgrew the working set
+// (small capacity only: nothing is written, the caller lists it for the full pass)
+template <int L, int K, class Mem>
+__device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, int p, Mem& M,
+                                         bool can_spill) {
+  const int2 pr = B.pairs[p];
+  typename SrcOf<L, K>::type src;
+  bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
+  GjkState g;
+  load_simplex(B.smp + p, B.dist[p], g);
+  EpaOut o;
+  epa_pair(t, src, B.cfg, g, M, o, can_spill);
+  if (o.spill) return false;
+  const bool lead = t.lane() == 0;
+  if (lead) {
+    B.dist[p] = o.dist;
+    gkSimplex* s = B.smp + p;
+    s->witnesses[0][0] = o.w0.x;
+    s->witnesses[0][1] = o.w0.y;
+    s->witnesses[0][2] = o.w0.z;
+    s->witnesses[1][0] = o.w1.x;
+    s->witnesses[1][1] = o.w1.y;
+    s->witnesses[1][2] = o.w1.z;
+    store3(B.nrm + 3 * (size_t)p, o.nrm);
+    if (B.status) B.status[p] = (B.mode == kModeEpa ? 0 : B.status[p]) | o.status;
+  }
+  const int q = warp_append(B.counts + kCntPolish, lead && o.polish);
+  if (lead && o.polish) {
+    PolishRec r;
+    r.pair = p;
+    r.kind = 1;
+    for (int k = 0; k < 3; ++k) {
+      r.face[k][0] = o.face[k][0];
+      r.face[k][1] = o.face[k][1];
+    }
+    B.polish[q] = r;
+  }
+  return true;
+}
+
+// EPA over one bucket's contacts with the small working set (EpaMemSmall per team in
+// shared memory); contacts that need more than kEpaSmallIters expansions go to the
+// spill list
 template <int L, int K>
 __global__ void __launch_bounds__(128) k_epa(DevBatch B, int bucket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  EpaMem* mem = reinterpret_cast<EpaMem*>(smem_raw);
+  EpaMemSmall* mem = reinterpret_cast<EpaMemSmall*>(smem_raw);
   const WarpTeam<L> t;
-  EpaMem& M = mem[threadIdx.x / L];
+  EpaMemSmall& M = mem[threadIdx.x / L];
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
   const int cnt = B.counts[kCntEpa + bucket];
   const int* list = B.elists + (size_t)bucket * B.npairs;
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
-    const int2 pr = B.pairs[p];
-    typename SrcOf<L, K>::type src;
-    bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
-    GjkState g;
-    load_simplex(B.smp + p, B.dist[p], g);
-    EpaOut o;
-    epa_pair(t, src, B.cfg, g, M, o);
+    const bool ok = epa_item<L, K>(t, B, p, M, B.cfg.epa_max_iter > kEpaSmallIters);
     const bool lead = t.lane() == 0;
-    if (lead) {
-      B.dist[p] = o.dist;
-      gkSimplex* s = B.smp + p;
-      s->witnesses[0][0] = o.w0.x;
-      s->witnesses[0][1] = o.w0.y;
-      s->witnesses[0][2] = o.w0.z;
-      s->witnesses[1][0] = o.w1.x;
-      s->witnesses[1][1] = o.w1.y;
-      s->witnesses[1][2] = o.w1.z;
-      store3(B.nrm + 3 * (size_t)p, o.nrm);
-      if (B.status) B.status[p] = (B.mode == kModeEpa ? 0 : B.status[p]) | o.status;
-    }
-    const int q = warp_append(B.counts + kCntPolish, lead && o.polish);
-    if (lead && o.polish) {
-      PolishRec r;
-      r.pair = p;
-      r.kind = 1;
-      for (int k = 0; k < 3; ++k) {
-        r.face[k][0] = o.face[k][0];
-        r.face[k][1] = o.face[k][1];
-      }
-      B.polish[q] = r;
-    }
+    const int q = warp_append(B.counts + kCntSpill, lead && !ok);
+    if (lead && !ok) B.spill[q] = p;
     t.sync();  // the next pair reuses M
   }
 }
@@ -254,11 +279,14 @@ int gjk_variants(const KernelInfo** out);
 int epa_variants(const KernelInfo** out);
 int gjk_variants_a(const KernelInfo** out);
 int gjk_variants_b(const KernelInfo** out);
+int gjk_variants_c(const KernelInfo** out);
 int epa_variants_a(const KernelInfo** out);
 int epa_variants_b(const KernelInfo** out);
 
 // non-template kernels (ogx_k_misc.cu)
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st);
+cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st);
+cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);
 cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st);

@@ -11,7 +11,7 @@
 // Limits and behaviour (also in include/ogx.h):
 //  * at most kNoAllocMaxPairs pairs per call; larger batches are rejected with
 //    OGX_ERR_CAPACITY;
-//  * the array (kNoAllocScratchBytes, 1,769,728 bytes) exists on every GPU that loads the
+//  * the array (kNoAllocScratchBytes, 1,835,264 bytes) exists on every GPU that loads the
 //    library, from load until the process exits;
 //  * every call uses the same array and the array keeps the last call's contents; the
 //    work-list counters must start at zero and each call clears them itself (a memset on
@@ -42,9 +42,10 @@ constexpr size_t kOffElists = kOffLists + (size_t)kBuckets * kNoAllocMaxPairs * 
 constexpr size_t kOffRefine = kOffElists + (size_t)kBuckets * kNoAllocMaxPairs * sizeof(int);
 constexpr size_t kOffRefineFull = kOffRefine + (size_t)kNoAllocMaxPairs * sizeof(RefineRec);
 constexpr size_t kOffPolish = kOffRefineFull + (size_t)kNoAllocMaxPairs * sizeof(int);
-constexpr size_t kNoAllocScratchBytes = kOffPolish + (size_t)kNoAllocMaxPairs * sizeof(PolishRec);
+constexpr size_t kOffSpill = kOffPolish + (size_t)kNoAllocMaxPairs * sizeof(PolishRec);
+constexpr size_t kNoAllocScratchBytes = kOffSpill + (size_t)kNoAllocMaxPairs * sizeof(int);
 
-static_assert(kNoAllocScratchBytes == 1769728, "the size is documented in include/ogx.h");
+static_assert(kNoAllocScratchBytes == 1835264, "the size is documented in include/ogx.h");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -54,7 +55,7 @@ struct Setup {
   KernelInfo gjk[kBuckets], epa[kBuckets];
   int grid_gjk[kBuckets], grid_epa[kBuckets];
   size_t smem_epa[kBuckets];
-  int grid_bin = 0, grid_refine = 0, grid_polish = 0;
+  int grid_bin = 0, grid_refine = 0, grid_polish = 0, grid_spill = 0;
 };
 
 std::mutex g_mu;
@@ -100,7 +101,7 @@ ogx_status setup(int dev, Setup** out) {
     if (!g || !q) return ogx_fail(OGX_ERR_CUDA, "no kernel variant for bucket %d", b);
     s.gjk[b] = *g;
     s.epa[b] = *q;
-    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * sizeof(EpaMem);  // 4 x 5.7 KB < 48 KB
+    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * sizeof(EpaMemSmall);  // < 48 KB
     int per = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, g->fn, kNoAllocBlock, 0);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy");
@@ -113,6 +114,9 @@ ogx_status setup(int dev, Setup** out) {
   e = refine_occupancy(kNoAllocBlock, &per);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy");
   s.grid_refine = std::max(1, per) * sms;
+  e = epa_spill_occupancy(kNoAllocBlock, &per);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy");
+  s.grid_spill = std::max(1, per) * sms;
   e = polish_occupancy(kNoAllocBlock, &per);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy");
   s.grid_polish = std::max(1, per) * sms;
@@ -166,6 +170,8 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
   B.refine = reinterpret_cast<RefineRec*>(S->scratch + kOffRefine);
   B.refine_full = reinterpret_cast<int*>(S->scratch + kOffRefineFull);
   B.polish = reinterpret_cast<PolishRec*>(S->scratch + kOffPolish);
+  B.spill = reinterpret_cast<int*>(S->scratch + kOffSpill);
+  B.warm = nullptr;
   B.cfg = c;
   B.mode = kModeGjkEpa;
 
@@ -182,6 +188,7 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
     S->epa[b].fn<<<S->grid_epa[b], kNoAllocBlock, S->smem_epa[b], s>>>(B, b);
     e = cudaGetLastError();
   }
+  if (e == cudaSuccess) e = launch_epa_spill(B, S->grid_spill, s);
   if (e == cudaSuccess && (c.flags & OGX_F_FP64_POLISH)) e = launch_polish(B, S->grid_polish, s);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "no-allocation pipeline launch");
   return OGX_OK;

@@ -136,12 +136,12 @@ class Context:
         return self.kernel_choice()
 
     def work_counts(self) -> dict:
-        c = (ctypes.c_int32 * 17)()
-        n = self.lib.ogx_ctx_work_counts(self.handle, c, 17)
-        if n != 17:
+        c = (ctypes.c_int32 * 18)()
+        n = self.lib.ogx_ctx_work_counts(self.handle, c, 18)
+        if n != 18:
             raise _lib.OgxError(-2, "work counts unavailable")
         return {"gjk": list(c[0:7]), "epa": list(c[7:14]), "polish": int(c[14]), "refine": int(c[15]),
-                "refine_full": int(c[16])}
+                "refine_full": int(c[16]), "epa_spill": int(c[17])}
 
 
 class Pool:

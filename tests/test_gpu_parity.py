@@ -63,3 +63,48 @@ def test_gjk_only_mode(engine, orc):
     enclosed = o["nvrtx"] == 4
     assert np.all(res["simplex"]["nvrtx"][enclosed] == 4)
     assert np.all(d[enclosed] == 0.0)
+
+
+def _variant_columns(ctx):
+    """For each bucket, the (lanes, blocks) variants the library accepts for it."""
+    from ogx import _lib
+    cols = {"gjk": [[] for _ in range(7)], "epa": [[] for _ in range(7)]}
+    for kind in ("gjk", "epa"):
+        for b in range(7):
+            for L in (1, 2, 4, 8, 16, 32):
+                for K in (0, 1, 2, 4):
+                    try:
+                        ctx.set_kernel_choice(kind, b, L, K)
+                    except _lib.OgxError:
+                        continue
+                    cols[kind][b].append((L, K))
+    return cols
+
+
+def test_every_variant_matches_host_build(engine, twin):
+    """The autotuner may pick any compiled variant for a bucket: each one must give the
+    host build's results (ranked slot order makes EPA independent of the team width)."""
+    import torch
+    b = W.powerlaw(seed=23, n_pairs=6000)
+    h = twin.run(b)
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    pool.upload(b.coords)
+    pairs = torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()
+    cols = _variant_columns(ctx)
+    width = max(len(c) for kind in cols.values() for c in kind)
+    tried = set()
+    for i in range(width):
+        for kind in ("gjk", "epa"):
+            for bk in range(7):
+                c = cols[kind][bk]
+                if c:
+                    L, K = c[min(i, len(c) - 1)]
+                    ctx.set_kernel_choice(kind, bk, L, K)
+                    tried.add((kind, bk, L, K))
+        g = engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA).to_host()
+        same = g["dist"] == h["dist"]
+        assert same.mean() > 0.995, (i, ctx.kernel_choice(), same.mean())
+        close = np.abs(g["dist"].astype(np.float64) - h["dist"]) <= 1e-6 * np.maximum(1, np.abs(h["dist"]))
+        assert close.mean() > 0.999, (i, ctx.kernel_choice())
+    assert len(tried) >= 20

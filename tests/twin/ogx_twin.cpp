@@ -30,7 +30,12 @@ struct Job {
   int32_t* iters;
 };
 
-void one(const Job& J, int i, EpaMem& M) {
+struct Work {
+  EpaMemSmall small;
+  EpaMem full;
+};
+
+void one(const Job& J, int i, Work& M) {
   const int b1 = J.pairs[2 * i], b2 = J.pairs[2 * i + 1];
   BodyRef A{J.quad[b1], J.counts[b1]}, Bb{J.quad[b2], J.counts[b2]};
   MemBodies B;
@@ -60,8 +65,10 @@ void one(const Job& J, int i, EpaMem& M) {
   int st = g.status, ei = 0;
   if (J.mode == 2) {
     if (contact) {
+      // as on the device: the small working set first, full capacity when it runs out
       EpaOut o;
-      epa_pair(t, B, *J.cfg, g, M, o);
+      epa_pair(t, B, *J.cfg, g, M.small, o, J.cfg->epa_max_iter > kEpaSmallIters);
+      if (o.spill) epa_pair(t, B, *J.cfg, g, M.full, o, false);
       if (o.polish) epa_polish(B, o);
       d = o.dist;
       w0 = o.w0;
@@ -94,7 +101,7 @@ void one(const Job& J, int i, EpaMem& M) {
 
 void* worker(void* arg) {
   const Job& J = *static_cast<const Job*>(arg);
-  EpaMem* M = new EpaMem;
+  Work* M = new Work;
   for (int i = J.lo; i < J.hi; ++i) one(J, i, *M);
   delete M;
   return nullptr;
