@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the kernel autotuner")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
     return ap.parse_args()
@@ -146,10 +147,89 @@ def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
                                    f"{threads} threads, {dt:.1f} s"}
 
 
+def serving_report(device: int, seed: int = 77) -> dict:
+    """Serving loop on 20k resident rigid bodies (log-uniform 8-512 vertices): ticks of
+    1k-200k candidate pairs (log-uniform) arrive as a Poisson process; each tick uploads
+    new poses and submits its pairs; latency = submit -> results in host memory.  Phase 1
+    mixes tick sizes at ~50% of the measured capacity, phase 2 sends only 200k-pair ticks
+    at ~50% of the capacity for them."""
+    import threading as th
+    from ogx import serving
+    from ogx import workloads as W
+    scene = W.serving_scene(seed=seed)
+    n_lists = 24
+    sizes = W.tick_sizes(seed, n_lists)
+    sizes[-6:] = 200_000
+    lists = [scene.candidate_pairs(t, int(n)) for t, n in enumerate(sizes)]
+    xfs = [scene.transforms(t) for t in range(n_lists)]
+    srv = serving.Server(scene.counts, scene.local, device=device, slots=4, slot_pairs=262144,
+                         max_pairs_in_flight=600_000, world_slots=8, warm_start=True)
+    try:
+        # capacity: back-to-back requests of each list, results waited in order
+        def burst(idx):
+            t0 = time.perf_counter()
+            reqs = []
+            for i in idx:
+                v = srv.set_transforms(xfs[i])
+                reqs.append(srv.submit(v, lists[i]))
+            for r in reqs:
+                srv.wait(r)
+            return time.perf_counter() - t0
+        burst(range(n_lists))  # warm-up (and warm-start table fill)
+        dt = burst(range(n_lists))
+        cap_pairs_s = float(sizes.sum()) / dt
+        big = [i for i in range(n_lists) if sizes[i] == 200_000]
+        dt_big = burst(big)
+        cap_big_hz = len(big) / dt_big
+
+        def run(phase_lists, rate_hz, n_ticks, seed2):
+            arrivals = W.poisson_arrivals(seed2, n_ticks, rate_hz)
+            order = np.random.default_rng(seed2).choice(phase_lists, size=n_ticks)
+            out = [None] * n_ticks
+            t0 = time.perf_counter() + 0.05
+
+            def submitter():
+                for k in range(n_ticks):
+                    while time.perf_counter() < t0 + arrivals[k]:
+                        time.sleep(5e-5)
+                    i = int(order[k])
+                    v = srv.set_transforms(xfs[i])
+                    out[k] = srv.submit(v, lists[i])
+            thr = th.Thread(target=submitter)
+            thr.start()
+            lat = []
+            for k in range(n_ticks):
+                while out[k] is None:
+                    time.sleep(5e-5)
+                lat.append(srv.wait(out[k]).latency_ms)
+            thr.join()
+            span = time.perf_counter() - t0
+            pairs = float(sum(sizes[int(i)] for i in order))
+            return np.array(lat), pairs / span
+
+        mix_rate = 0.5 * cap_pairs_s / float(sizes.mean())
+        lat_mix, thr_mix = run(list(range(n_lists)), mix_rate, 300, seed + 1)
+        big_rate = 0.5 * cap_big_hz
+        lat_big, thr_big = run(big, big_rate, 100, seed + 2)
+    finally:
+        srv.close()
+    return {
+        "bodies": scene.n_bodies, "mean_vertices": float(scene.counts.mean()),
+        "tick_pairs": "log-uniform [1k, 200k] (phase 1), 200k (phase 2)",
+        "arrivals": "Poisson", "warm_start": True, "slots": 4, "max_pairs_in_flight": 600_000,
+        "capacity_pairs_per_s": cap_pairs_s, "capacity_200k_ticks_per_s": cap_big_hz,
+        "mixed": {"rate_hz": mix_rate, "ticks": len(lat_mix), "pairs_per_s": thr_mix,
+                  "p50_ms": float(np.percentile(lat_mix, 50)), "p99_ms": float(np.percentile(lat_mix, 99))},
+        "ticks_200k": {"rate_hz": big_rate, "ticks": len(lat_big), "pairs_per_s": thr_big,
+                       "p50_ms": float(np.percentile(lat_big, 50)), "p99_ms": float(np.percentile(lat_big, 99))},
+        "latency": "submit -> results in host memory, host clock",
+    }
+
+
 def load_traffic() -> dict:
-    """DRAM bytes per work unit of each kernel, from the committed ncu summary
-    (profiles/dram_traffic.json: dram__bytes_read.sum + dram__bytes_write.sum of one
-    captured launch divided by the units it processed)."""
+    """DRAM traffic of each kernel relative to its algorithmic bytes, from the committed
+    ncu summary (profiles/dram_traffic.json: dram__bytes_read.sum + dram__bytes_write.sum
+    of one captured launch over the algorithmic bytes of the units it processed)."""
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
             return json.load(f)
@@ -343,8 +423,8 @@ def run_ours(args):
     achieved = dom_bytes / (fam_ms[dom] / 1e3) / 1e9
     traffic = None
     tr = load_traffic().get(dom)
-    if tr and units:
-        traffic = tr["bytes_per_unit"] * units / fam_n[dom]
+    if tr:
+        traffic = tr["traffic_over_algorithmic"] * dom_bytes / fam_n[dom]
     pipeline_gbs = alg_bytes / (ms / 1e3) / 1e9
     roof = {"bound": "hbm", "kernel": f"{dom} ({fam_n[dom]} bucket launches)", "achieved": achieved,
             "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
@@ -373,6 +453,11 @@ def run_ours(args):
         line["e2e"] = e2e
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(batch)
+    if not args.no_serving:
+        del out, pairs
+        pool.close()
+        torch.cuda.empty_cache()
+        line["serving"] = serving_report(local)
     print(json.dumps(line), flush=True)
     pool.close()
     ctx.close()

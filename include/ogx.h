@@ -40,6 +40,7 @@ typedef int ogx_status;
 #define OGX_ERR_NOMEM (-3)     /* device or pinned host allocation failed */
 #define OGX_ERR_NO_DEVICE (-4) /* no usable GPU */
 #define OGX_ERR_CAPACITY (-5)  /* a size exceeds a capacity of the call */
+#define OGX_ERR_BUSY (-6)      /* a wait timed out (serving loop) */
 
 /* Run-time tolerances.  ogx_config_default() fills the engine defaults (FP32 bulk,
  * FP64 escalation and polish, distances to ~1e-5 relative of the FP64 oracle);
@@ -139,7 +140,8 @@ int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
  * per EPA bucket [7, 14), EPA faces re-solved in FP64 [14], pairs whose GJK result was
  * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16],
  * contacts whose EPA outgrew the bucket kernels' working set and ran again at full
- * capacity [17].  cap must be >= 18. */
+ * capacity [17], FP64 continuations of pairs with a body above 128 points (one warp
+ * each; the others in [16] - [18] run one thread each) [18].  cap must be >= 19. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 /* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most
@@ -172,6 +174,55 @@ ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_bodies, int 
                                int npairs, const gkCollisionPair* d_pairs,
                                gkSimplex* d_simplices, float* d_distances, float* d_normals,
                                int32_t* d_status, const ogx_config* cfg, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Serving loop.  No counterpart in the reference's library: its per-frame path  */
+/* (visualization/integrate_final_gjk.cu:1028-1037) moves every body on the host */
+/* and calls the indexed functions synchronously.  A server keeps the bodies on  */
+/* the device in their own frame; each transform update writes a world-space     */
+/* copy (one of `world_slots` ring buffers, identified by a version); requests   */
+/* (the candidate pairs of one tick) are queued and admitted oldest first as     */
+/* soon as a slot (stream + buffers for slot_pairs pairs) is free and the pairs  */
+/* in flight stay within max_pairs_in_flight; admitted requests run concurrently.*/
+/* Warm starts: the first vertex pair of the last simplex of each (i, j) pair is */
+/* kept in a device hash table and GJK starts there.                             */
+
+typedef struct ogx_server ogx_server;
+typedef struct ogx_server_config {
+  int slots;               /* requests on the device at once (one stream each) */
+  int slot_pairs;          /* largest request, in pairs */
+  int max_pairs_in_flight; /* admission budget over all running requests */
+  int world_slots;         /* world-space copies of the pool (transform versions kept) */
+  int warm_start;          /* 1: warm-start GJK from the previous simplex of the pair */
+  int warm_capacity_log2;  /* warm-start table entries (16 B each) */
+} ogx_server_config;
+
+void ogx_server_config_default(ogx_server_config* sc);
+/* Bodies in their own frame: counts[num_bodies], local_xyz = concatenated xyz. */
+ogx_status ogx_server_create(int device, const ogx_config* cfg, const ogx_server_config* sc,
+                             int num_bodies, const int32_t* counts, const float* local_xyz,
+                             ogx_server** out);
+ogx_status ogx_server_destroy(ogx_server* server);
+/* New poses: xf[num_bodies][12] = row-major rotation R (9) then translation t (3); the
+ * world point is R p + t evaluated in double and rounded once to float.  Returns the
+ * version to submit requests against.  Blocks (at most 10 s, then OGX_ERR_BUSY) while
+ * the ring slot it overwrites is still used by a queued or running request. */
+ogx_status ogx_server_set_transforms(ogx_server* server, const float* xf, int64_t* version);
+/* Queue a request: npairs <= slot_pairs pairs of body indices (copied at once); the
+ * results are written to the host arrays (any of them may be NULL) before the request
+ * completes, so they must stay valid until ogx_server_wait returns.  Page-locked arrays
+ * (cudaMallocHost, cudaHostRegister) receive the results directly from the device;
+ * others through the server's pinned staging and one host copy. */
+ogx_status ogx_server_submit(ogx_server* server, int64_t version, int npairs,
+                             const gkCollisionPair* pairs, gkSimplex* simplices,
+                             float* distances, float* normals, int32_t* status, int64_t* ticket);
+ogx_status ogx_server_poll(ogx_server* server, int64_t ticket, int* done);
+/* Wait for a request (timeout_s <= 0: no limit); latency_ms = completion - submission
+ * on the host clock.  The ticket is released. */
+ogx_status ogx_server_wait(ogx_server* server, int64_t ticket, double timeout_s, double* latency_ms);
+/* Device layout of the world-space pool of a version (for checks and custom kernels). */
+ogx_status ogx_server_world_layout(ogx_server* server, int64_t version, float** d_points,
+                                   void** d_bodies);
 
 /* ------------------------------------------------------------------------- */
 /* Reference-compatible entry points.  Same arguments, meaning and output     */

@@ -108,7 +108,7 @@ bool g_tuned_valid[16];
 
 // can variant v serve bucket b?
 bool serves(const Launch& v, int b) {
-  if (v.K == 0) return b >= 4;  // memory-streamed: only worth trying for large bodies
+  if (v.K == 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
   if (b == kBuckets - 1) return false;
   const int cap = 4 * v.L * v.K;
   return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];
@@ -160,9 +160,13 @@ ogx_status init_kernels(int device) {
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = gjk_variants_c(&t);
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = gjk_variants_d(&t);
+  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_a(&t);
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_b(&t);
+  for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = epa_variants_c(&t);
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   for (auto& k : g_gjkv) {
     ogx_status s = init_variant(&k, false, sms);
@@ -580,7 +584,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     ctx->mark("refine");
     e = launch_refine(B, g_grid_refine, g_grid_pack, st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
-    launches += 2;
+    launches += 3;
   }
   if (mode != kModeGjk) {
     for (int b = kBuckets - 1; b >= 0; --b) {

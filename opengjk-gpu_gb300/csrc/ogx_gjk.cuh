@@ -787,143 +787,182 @@ OGX_HD int exact_support(const Team& t, const Bodies& B, int w, dv3 d, double& v
 }
 
 // FP64 continuation of GJK from the FP32 result: exact supports, FP64 sub-distance,
-// stop when the FP64 gap |v|^2 - v.w <= 1e-13 |v|^2 or the support repeats.  Certifies
+// stop when the FP64 gap |v|^2 - v.w <= 1e-12 |v|^2 or the support repeats.  Certifies
 // (or corrects) the FP32 answer; sets g.n = 4 if the origin turns out to be enclosed.
-template <class Team, class Bodies>
-OGX_HD void gjk_refine(const Team& t, const Bodies& B, GjkState& g, int max_iter) {
-  const bool certain = g.certain;
+// Split in three so that a warp can run the supports of 32 pairs cooperatively while
+// each lane keeps its own pair's state (refine_begin, then refine_step with the exact
+// supports along -v / v until done, then refine_end).
+struct RefineState {
   Sx<double> s;
   int ia[4], ib[4];
+  dv3 v;
+  double wmax2;
+  int it, max_iter;
+  bool done, enclosed;
+};
+
+template <class Bodies>
+OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, RefineState& r) {
+  Sx<double>& s = r.s;
   s.n = g.n > 3 ? 3 : g.n;
   for (int j = 0; j < s.n; ++j) {
-    ia[j] = g.ia[j];
-    ib[j] = g.ib[j];
-    s.v[j].p = B.dpoint(0, ia[j]) - B.dpoint(1, ib[j]);
+    r.ia[j] = g.ia[j];
+    r.ib[j] = g.ib[j];
+    s.v[j].p = B.dpoint(0, r.ia[j]) - B.dpoint(1, r.ib[j]);
     s.v[j].k = j;
   }
   // exact closest point of the FP32 result's simplex; keep only the vertices it uses
   dv3 P[3];
   for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
   double lam[4];
-  dv3 v;
-  closest_on_simplex(s.n, P, lam, v);
+  closest_on_simplex(s.n, P, lam, r.v);
   {
-    Sx<double> r;
-    r.n = 0;
-    int ra[4], rb[4];
+    Sx<double> q;
+    q.n = 0;
+    int qa[4], qb[4];
     for (int j = 0; j < s.n; ++j)
       if (lam[j] > 0.0 || (s.n == 1)) {
-        r.v[r.n] = s.v[j];
-        ra[r.n] = ia[j];
-        rb[r.n] = ib[j];
-        r.n++;
+        q.v[q.n] = s.v[j];
+        qa[q.n] = r.ia[j];
+        qb[q.n] = r.ib[j];
+        q.n++;
       }
-    if (r.n == 0) {
-      r.v[0] = s.v[0];
-      ra[0] = ia[0];
-      rb[0] = ib[0];
-      r.n = 1;
+    if (q.n == 0) {
+      q.v[0] = s.v[0];
+      qa[0] = r.ia[0];
+      qb[0] = r.ib[0];
+      q.n = 1;
     }
-    s = r;
+    s = q;
     for (int j = 0; j < s.n; ++j) {
-      ia[j] = ra[j];
-      ib[j] = rb[j];
+      r.ia[j] = qa[j];
+      r.ib[j] = qb[j];
       s.v[j].k = j;
     }
   }
-  int it = 0;
-  bool enclosed = false;
-  double wmax2 = 0.0;
-  for (int j = 0; j < s.n; ++j) wmax2 = fmax(wmax2, dot(s.v[j].p, s.v[j].p));
-  if (certain) it = max_iter + 1;  // the FP32 pass proved the simplex final
-  for (; it < max_iter; ++it) {
-    double va, vb;
-    const int xa = exact_support(t, B, 0, -v, va);
-    const int xb = exact_support(t, B, 1, v, vb);
-    const dv3 w = B.dpoint(0, xa) - B.dpoint(1, xb);
-    const double vv = dot(v, v);
-    // FP64 gap test.  In exact arithmetic v.p_j = |v|^2 for every vertex p_j of the
-    // current feature, so the gap |v|^2 - v.w equals v.(p_j - w); that form rounds in
-    // proportion to |p_j - w| (small near convergence) instead of |w|^2.  Relative
-    // tolerance of the FP64 oracle (eps * 1e4) and a rounding floor.
-    double gap = INFINITY, dmax = 0.0;
-    for (int j = 0; j < s.n; ++j) {
-      const dv3 e = s.v[j].p - w;
-      gap = fmin(gap, dot(v, e));
-      dmax = fmax(dmax, dot(e, e));
-    }
-    const double floor64 = 64.0 * DBL_EPSILON * sqrt(wmax2) * sqrt(dmax);
-#ifdef OGX_TRACE
-    printf("refine it %d: n=%d |v|=%.12g support (%d,%d) gap %.3g floor %.3g\n", it, s.n, sqrt(vv), xa, xb, gap, floor64);
-#endif
-    if (gap <= 1e-12 * vv || gap <= floor64) break;
-    bool dup = false;
-    for (int j = 0; j < s.n; ++j) dup |= (ia[j] == xa && ib[j] == xb);
-    if (dup) break;
-    const Sx<double> prev = s;
-    int pa[4], pb[4];
-    for (int j = 0; j < s.n; ++j) {
-      pa[j] = ia[j];
-      pb[j] = ib[j];
-    }
-    const dv3 vprev = v;
-    s.v[s.n].p = w;
-    s.v[s.n].k = s.n;
-    ia[s.n] = xa;
-    ib[s.n] = xb;
-    s.n++;
-    Unc u{false};
-    subdistance(s, v, u);
-    if (s.n != 4 && !(dot(v, v) < vv * (1.0 - 1e-12))) {
-      // no progress: a tie support spanning a degenerate simplex -- keep the last answer
-      s = prev;
-      v = vprev;
-      for (int j = 0; j < s.n; ++j) {
-        ia[j] = pa[j];
-        ib[j] = pb[j];
-      }
-      break;
-    }
-    int na[4], nb[4];
-    for (int j = 0; j < s.n; ++j) {
-      na[j] = ia[s.v[j].k];
-      nb[j] = ib[s.v[j].k];
-    }
-    for (int j = 0; j < s.n; ++j) {
-      ia[j] = na[j];
-      ib[j] = nb[j];
-      s.v[j].k = j;
-      wmax2 = fmax(wmax2, dot(s.v[j].p, s.v[j].p));
-    }
-    if (s.n == 4) {
-      enclosed = true;
-      break;
-    }
+  r.wmax2 = 0.0;
+  for (int j = 0; j < s.n; ++j) r.wmax2 = fmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
+  r.max_iter = max_iter;
+  r.enclosed = false;
+  r.it = g.certain ? max_iter + 1 : 0;  // the FP32 pass proved the simplex final
+  r.done = r.it >= max_iter;
+}
+
+// one FP64 iteration with the exact supports xa (body 1 along -v) and xb (body 2 along v)
+template <class Bodies>
+OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
+  Sx<double>& s = r.s;
+  const dv3 w = B.dpoint(0, xa) - B.dpoint(1, xb);
+  const double vv = dot(r.v, r.v);
+  // FP64 gap test.  In exact arithmetic v.p_j = |v|^2 for every vertex p_j of the
+  // current feature, so the gap |v|^2 - v.w equals v.(p_j - w); that form rounds in
+  // proportion to |p_j - w| (small near convergence) instead of |w|^2.  Relative
+  // tolerance of the FP64 oracle (eps * 1e4) and a rounding floor.
+  double gap = INFINITY, dmax = 0.0;
+  for (int j = 0; j < s.n; ++j) {
+    const dv3 e = s.v[j].p - w;
+    gap = fmin(gap, dot(r.v, e));
+    dmax = fmax(dmax, dot(e, e));
   }
+  const double floor64 = 64.0 * DBL_EPSILON * sqrt(r.wmax2) * sqrt(dmax);
+  if (gap <= 1e-12 * vv || gap <= floor64) {
+    r.done = true;
+    return;
+  }
+  bool dup = false;
+  for (int j = 0; j < s.n; ++j) dup |= (r.ia[j] == xa && r.ib[j] == xb);
+  if (dup) {
+    r.done = true;
+    return;
+  }
+  const Sx<double> prev = s;
+  int pa[4], pb[4];
+  for (int j = 0; j < s.n; ++j) {
+    pa[j] = r.ia[j];
+    pb[j] = r.ib[j];
+  }
+  const dv3 vprev = r.v;
+  s.v[s.n].p = w;
+  s.v[s.n].k = s.n;
+  r.ia[s.n] = xa;
+  r.ib[s.n] = xb;
+  s.n++;
+  Unc u{false};
+  subdistance(s, r.v, u);
+  if (s.n != 4 && !(dot(r.v, r.v) < vv * (1.0 - 1e-12))) {
+    // no progress: a tie support spanning a degenerate simplex -- keep the last answer
+    s = prev;
+    r.v = vprev;
+    for (int j = 0; j < s.n; ++j) {
+      r.ia[j] = pa[j];
+      r.ib[j] = pb[j];
+    }
+    r.done = true;
+    return;
+  }
+  int na[4], nb[4];
+  for (int j = 0; j < s.n; ++j) {
+    na[j] = r.ia[s.v[j].k];
+    nb[j] = r.ib[s.v[j].k];
+  }
+  for (int j = 0; j < s.n; ++j) {
+    r.ia[j] = na[j];
+    r.ib[j] = nb[j];
+    s.v[j].k = j;
+    r.wmax2 = fmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
+  }
+  if (s.n == 4) {
+    r.enclosed = true;
+    r.done = true;
+    return;
+  }
+  ++r.it;
+  if (r.it >= r.max_iter) r.done = true;
+}
+
+template <class Bodies>
+OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
+  const Sx<double>& s = r.s;
   g.n = s.n;
   for (int j = 0; j < s.n; ++j) {
-    g.ia[j] = ia[j];
-    g.ib[j] = ib[j];
+    g.ia[j] = r.ia[j];
+    g.ib[j] = r.ib[j];
     g.P[j] = cvt<float>(s.v[j].p);
   }
-  g.status |= (it == max_iter + 1) ? OGX_S_POLISHED : (OGX_S_POLISHED | OGX_S_GJK_ESCALATED);
-  if (it == max_iter) g.status |= OGX_S_GJK_CAP;
-  if (enclosed) {
+  g.status |= (r.it == r.max_iter + 1) ? OGX_S_POLISHED : (OGX_S_POLISHED | OGX_S_GJK_ESCALATED);
+  if (r.it == r.max_iter) g.status |= OGX_S_GJK_CAP;
+  if (r.enclosed) {
     g.v = v3<float>(0.f, 0.f, 0.f);
     g.dist = 0.0f;
     return;
   }
+  dv3 P[3];
   for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
+  double lam[4];
+  dv3 v;
   closest_on_simplex(s.n, P, lam, v);
   dv3 w0 = v3<double>(0.0, 0.0, 0.0), w1 = w0;
   for (int j = 0; j < s.n; ++j) {
-    w0 = w0 + B.dpoint(0, ia[j]) * lam[j];
-    w1 = w1 + B.dpoint(1, ib[j]) * lam[j];
+    w0 = w0 + B.dpoint(0, r.ia[j]) * lam[j];
+    w1 = w1 + B.dpoint(1, r.ib[j]) * lam[j];
   }
   g.v = cvt<float>(v);
   g.dist = (float)sqrt(dot(v, v));
   g.w0 = cvt<float>(w0);
   g.w1 = cvt<float>(w1);
+}
+
+template <class Team, class Bodies>
+OGX_HD void gjk_refine(const Team& t, const Bodies& B, GjkState& g, int max_iter) {
+  RefineState r;
+  refine_begin(B, g, max_iter, r);
+  while (!r.done) {
+    double va, vb;
+    const int xa = exact_support(t, B, 0, -r.v, va);
+    const int xb = exact_support(t, B, 1, r.v, vb);
+    refine_step(B, r, xa, xb);
+  }
+  refine_end(B, r, g);
 }
 
 // FP64 re-solve of the final simplex: exact Minkowski points, exact closest point.

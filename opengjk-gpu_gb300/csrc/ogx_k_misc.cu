@@ -107,14 +107,19 @@ __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   const int cnt = B.counts[kCntRefine];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const RefineRec rr = B.refine[k];
-    if (!rr.certain) {
-      const int q = atomicAdd(B.counts + kCntRefineFull, 1);
-      B.refine_full[q] = rr.pair;
-      continue;
-    }
     const int p = rr.pair;
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
+    if (!rr.certain) {
+      if ((ra.n > rb.n ? ra.n : rb.n) <= kRefineLaneMax) {
+        const int q = atomicAdd(B.counts + kCntRefineFull, 1);
+        B.refine_full[q] = p;
+      } else {
+        const int q = atomicAdd(B.counts + kCntRefineBig, 1);
+        B.refine_full[B.npairs - 1 - q] = p;
+      }
+      continue;
+    }
     MemBodies mb;
     mb.bind(B.pool, ra, rb);
     GjkState g;
@@ -126,14 +131,12 @@ __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   }
 }
 
-// FP64 continuation of GJK for the pairs with an uncertain FP32 support: one warp per
-// pair, the exact-support scans split over the lanes.
-__global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
-  const WarpTeam<32> t;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+// FP64 continuation of GJK for the pairs with an uncertain FP32 support and bodies of
+// at most kRefineLaneMax points: one thread per pair, so that each FP64 instruction
+// serves 32 pairs (FP64 issues at 1/64 of the FP32 rate here).
+__global__ void __launch_bounds__(128) k_refine_lane(DevBatch B) {
   const int cnt = B.counts[kCntRefineFull];
-  for (int k = warp; k < cnt; k += nwarps) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const int p = B.refine_full[k];
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
@@ -142,9 +145,72 @@ __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
     GjkState g;
     load_simplex(B.smp + p, B.dist[p], g);
     g.certain = false;
-    gjk_refine(t, mb, g, kRefineIters);
-    if (t.lane() == 0) refine_store(B, p, ra, rb, g);
-    __syncwarp();
+    SerialTeam one;
+    gjk_refine(one, mb, g, kRefineIters);
+    refine_store(B, p, ra, rb, g);
+  }
+}
+
+// The same for larger bodies: a warp takes 32 pairs, one per lane; each FP64 iteration
+// runs the exact-support scans of every unfinished pair with all 32 lanes (pair j's
+// bodies and direction broadcast from lane j), then each lane takes its own pair's FP64
+// sub-distance step, so the scalar FP64 work serves 32 pairs per instruction.
+__global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
+  const WarpTeam<32> t;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int cnt = B.counts[kCntRefineBig];
+  for (int base = 32 * warp; base < cnt; base += 32 * nwarps) {
+    const int k = base + lane;
+    const bool valid = k < cnt;
+    int p = -1;
+    BodyRef ra{0u, 1}, rb{0u, 1};
+    MemBodies mb;
+    mb.bind(B.pool, ra, rb);
+    GjkState g;
+    RefineState r;
+    r.done = true;
+    if (valid) {
+      p = B.refine_full[B.npairs - 1 - k];
+      const int2 pr = B.pairs[p];
+      ra = B.bodies[pr.x];
+      rb = B.bodies[pr.y];
+      mb.bind(B.pool, ra, rb);
+      load_simplex(B.smp + p, B.dist[p], g);
+      g.certain = false;
+      refine_begin(mb, g, kRefineIters, r);
+    }
+    for (;;) {
+      const unsigned m = __ballot_sync(full, !r.done);
+      if (m == 0u) break;
+      int my_xa = 0, my_xb = 0;
+      for (unsigned mm = m; mm != 0u; mm &= mm - 1u) {
+        const int j = __ffs(mm) - 1;
+        MemBodies bj;
+        for (int w = 0; w < 2; ++w) {
+          bj.base[w] = reinterpret_cast<const float*>(
+              __shfl_sync(full, reinterpret_cast<long long>(mb.base[w]), j));
+          bj.n[w] = __shfl_sync(full, mb.n[w], j);
+          bj.n4[w] = __shfl_sync(full, mb.n4[w], j);
+        }
+        const dv3 vj = v3<double>(__shfl_sync(full, r.v.x, j), __shfl_sync(full, r.v.y, j),
+                                  __shfl_sync(full, r.v.z, j));
+        double va, vb;
+        const int xa = exact_support(t, bj, 0, -vj, va);
+        const int xb = exact_support(t, bj, 1, vj, vb);
+        if (lane == j) {
+          my_xa = xa;
+          my_xb = xb;
+        }
+      }
+      if (!r.done) refine_step(mb, r, my_xa, my_xb);
+    }
+    if (valid) {
+      refine_end(mb, r, g);
+      refine_store(B, p, ra, rb, g);
+    }
   }
 }
 
@@ -227,6 +293,7 @@ cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
 
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st) {
   k_refine<<<grid, 128, 0, st>>>(B);
+  k_refine_lane<<<grid, 128, 0, st>>>(B);
   k_refine_full<<<grid_full, 128, 0, st>>>(B);
   return cudaGetLastError();
 }

@@ -51,7 +51,11 @@ constexpr int kCntPolish = 2 * kBuckets;    // EPA faces to re-solve in FP64
 constexpr int kCntRefine = 2 * kBuckets + 1;  // separated pairs to refine in FP64
 constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to continue in FP64
 constexpr int kCntSpill = 2 * kBuckets + 3;  // contacts that outgrew the small EPA capacity
-constexpr int kCntSlots = 2 * kBuckets + 4;
+constexpr int kCntRefineBig = 2 * kBuckets + 4;  // of the FP64 continuations, bodies > 128 points
+constexpr int kCntSlots = 2 * kBuckets + 5;
+// FP64 continuations of pairs whose bodies have at most this many points run one thread
+// per pair (FP64 instructions then serve 32 pairs); larger ones one warp per pair
+constexpr int kRefineLaneMax = 128;
 constexpr int kRefineIters = 16;
 
 struct DevBatch {
@@ -70,6 +74,7 @@ struct DevBatch {
   PolishRec* polish;
   RefineRec* refine;  // npairs entries
   int* refine_full;   // npairs entries: pair ids whose FP32 support was not certain
+                      // (small bodies from the front, large ones from the back)
   int* spill;         // npairs entries: contacts to re-run at full EPA capacity
   const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
   ogx_config cfg;
@@ -280,8 +285,10 @@ int epa_variants(const KernelInfo** out);
 int gjk_variants_a(const KernelInfo** out);
 int gjk_variants_b(const KernelInfo** out);
 int gjk_variants_c(const KernelInfo** out);
+int gjk_variants_d(const KernelInfo** out);
 int epa_variants_a(const KernelInfo** out);
 int epa_variants_b(const KernelInfo** out);
+int epa_variants_c(const KernelInfo** out);
 
 // non-template kernels (ogx_k_misc.cu)
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st);

@@ -1,0 +1,152 @@
+"""Python handle on the engine's serving loop (ogx_server_* in include/ogx.h).
+
+A server keeps the bodies on the GPU in their own frame, takes pose updates
+(``set_transforms``, one version per tick) and pair requests (``submit``), admits
+queued requests as device slots and the in-flight pair budget allow, runs them
+concurrently and returns each request's results and its submit-to-done latency.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+P = ctypes.c_void_p
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int), ("slot_pairs", ctypes.c_int), ("max_pairs_in_flight", ctypes.c_int),
+                ("world_slots", ctypes.c_int), ("warm_start", ctypes.c_int), ("warm_capacity_log2", ctypes.c_int)]
+
+
+def _bind(lib):
+    if getattr(lib, "_ogx_server_bound", False):
+        return
+    I64 = ctypes.c_int64
+    lib.ogx_server_config_default.restype = None
+    lib.ogx_server_config_default.argtypes = [P]
+    lib.ogx_server_create.restype = ctypes.c_int
+    lib.ogx_server_create.argtypes = [ctypes.c_int, P, P, ctypes.c_int, P, P, P]
+    lib.ogx_server_destroy.restype = ctypes.c_int
+    lib.ogx_server_destroy.argtypes = [P]
+    lib.ogx_server_set_transforms.restype = ctypes.c_int
+    lib.ogx_server_set_transforms.argtypes = [P, P, ctypes.POINTER(I64)]
+    lib.ogx_server_submit.restype = ctypes.c_int
+    lib.ogx_server_submit.argtypes = [P, I64, ctypes.c_int, P, P, P, P, P, ctypes.POINTER(I64)]
+    lib.ogx_server_poll.restype = ctypes.c_int
+    lib.ogx_server_poll.argtypes = [P, I64, ctypes.POINTER(ctypes.c_int)]
+    lib.ogx_server_wait.restype = ctypes.c_int
+    lib.ogx_server_wait.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    lib.ogx_server_world_layout.restype = ctypes.c_int
+    lib.ogx_server_world_layout.argtypes = [P, I64, ctypes.POINTER(P), ctypes.POINTER(P)]
+    lib._ogx_server_bound = True
+
+
+def _pinned(nbytes: int):
+    """Page-locked host buffer (torch's caching pinned allocator) and its numpy view."""
+    import torch
+    t = torch.empty(max(nbytes, 16), dtype=torch.uint8, pin_memory=True)
+    return t, t.numpy()[:nbytes]
+
+
+class Request:
+    """Host result arrays of one submitted request (filled when it completes).  They are
+    page-locked, so the device writes them directly."""
+
+    def __init__(self, ticket: int, pairs: np.ndarray, n: int):
+        self.ticket = ticket
+        self.pairs = pairs
+        self._bufs = []
+
+        def arr(dtype, shape):
+            dt = np.dtype(dtype)
+            t, raw = _pinned(int(np.prod(shape)) * dt.itemsize)
+            self._bufs.append(t)
+            return raw.view(dt).reshape(shape)
+        self.dist = arr(np.float32, (n,))
+        self.simplex = arr(_lib.SIMPLEX_DTYPE, (n,))
+        self.normal = arr(np.float32, (n, 3))
+        self.status = arr(np.int32, (n,))
+        self.latency_ms = None
+
+    def results(self) -> dict:
+        return {"dist": self.dist, "simplex": self.simplex, "normal": self.normal, "status": self.status}
+
+
+class Server:
+    def __init__(self, counts, local_xyz, config: _lib.Config | None = None, device: int = 0, slots: int = 4,
+                 slot_pairs: int = 262144, max_pairs_in_flight: int = 1 << 20, world_slots: int = 4,
+                 warm_start: bool = True, warm_capacity_log2: int = 22):
+        self.lib = _lib.load()
+        _bind(self.lib)
+        sc = ServerConfig()
+        self.lib.ogx_server_config_default(ctypes.byref(sc))
+        sc.slots, sc.slot_pairs, sc.max_pairs_in_flight = slots, slot_pairs, max_pairs_in_flight
+        sc.world_slots, sc.warm_start, sc.warm_capacity_log2 = world_slots, int(warm_start), warm_capacity_log2
+        self.counts = np.ascontiguousarray(counts, np.int32)
+        local = np.ascontiguousarray(local_xyz, np.float32)
+        h = P()
+        rc = self.lib.ogx_server_create(device, ctypes.byref(config) if config is not None else None,
+                                        ctypes.byref(sc), int(self.counts.shape[0]), self.counts.ctypes.data,
+                                        local.ctypes.data, ctypes.byref(h))
+        _lib.check(rc)
+        self.handle = h
+        self._live = {}
+
+    def set_transforms(self, xf: np.ndarray) -> int:
+        xf = np.ascontiguousarray(xf, np.float32)
+        assert xf.shape == (self.counts.shape[0], 12)
+        v = ctypes.c_int64()
+        _lib.check(self.lib.ogx_server_set_transforms(self.handle, xf.ctypes.data, ctypes.byref(v)))
+        return v.value
+
+    def submit(self, version: int, pairs: np.ndarray) -> Request:
+        pairs = np.ascontiguousarray(pairs, np.int32)
+        n = int(pairs.shape[0])
+        t = ctypes.c_int64()
+        req = Request(0, pairs, n)
+        _lib.check(self.lib.ogx_server_submit(self.handle, int(version), n, pairs.ctypes.data,
+                                              req.simplex.ctypes.data, req.dist.ctypes.data,
+                                              req.normal.ctypes.data, req.status.ctypes.data, ctypes.byref(t)))
+        req.ticket = t.value
+        self._live[req.ticket] = req  # the arrays must outlive the request
+        return req
+
+    def done(self, req: Request) -> bool:
+        d = ctypes.c_int()
+        _lib.check(self.lib.ogx_server_poll(self.handle, req.ticket, ctypes.byref(d)))
+        return bool(d.value)
+
+    def wait(self, req: Request, timeout_s: float = 60.0) -> Request:
+        lat = ctypes.c_double()
+        rc = self.lib.ogx_server_wait(self.handle, req.ticket, float(timeout_s), ctypes.byref(lat))
+        self._live.pop(req.ticket, None)
+        _lib.check(rc)
+        req.latency_ms = lat.value
+        return req
+
+    def world_layout(self, version: int):
+        pts, bodies = P(), P()
+        _lib.check(self.lib.ogx_server_world_layout(self.handle, int(version), ctypes.byref(pts),
+                                                    ctypes.byref(bodies)))
+        return pts.value, bodies.value
+
+    def close(self):
+        if self.handle:
+            self.lib.ogx_server_destroy(self.handle)
+            self.handle = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

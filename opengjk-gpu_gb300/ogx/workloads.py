@@ -351,3 +351,102 @@ REGISTRY = {
     "sphere_shell": sphere_shell,
     "stress": stress,
 }
+
+
+# ---------------------------------------------------------------------------------
+# serving scene: resident rigid bodies moving in a box, candidate pairs per tick
+
+@dataclasses.dataclass
+class Scene:
+    """Bodies in their own frame plus their motion.  Body b has counts[b] points
+    (local, float32, concatenated in `local`), starts at pos0[b] with orientation rot0[b]
+    and moves with velocity vel[b] (reflected at the walls of the box [-half, half]^3)
+    and angular velocity omg[b]."""
+    local: np.ndarray
+    counts: np.ndarray
+    offsets: np.ndarray
+    pos0: np.ndarray
+    vel: np.ndarray
+    rot0: np.ndarray
+    omg: np.ndarray
+    half: float
+    dt: float
+
+    @property
+    def n_bodies(self) -> int:
+        return int(self.counts.shape[0])
+
+    def poses(self, tick: int):
+        """Rotation matrices (B, 3, 3) and positions (B, 3) at `tick`, float64."""
+        t = tick * self.dt
+        span = 2.0 * self.half
+        p = self.pos0 + self.vel * t + self.half  # in [0, 2 half) before folding
+        p = np.mod(p, 2.0 * span)
+        p = np.where(p > span, 2.0 * span - p, p) - self.half
+        ang = np.linalg.norm(self.omg, axis=1) * t
+        axis = self.omg / np.maximum(np.linalg.norm(self.omg, axis=1, keepdims=True), 1e-300)
+        c, s = np.cos(ang)[:, None, None], np.sin(ang)[:, None, None]
+        x, y, z = axis[:, 0], axis[:, 1], axis[:, 2]
+        K = np.zeros((self.n_bodies, 3, 3))
+        K[:, 0, 1], K[:, 0, 2], K[:, 1, 0] = -z, y, z
+        K[:, 1, 2], K[:, 2, 0], K[:, 2, 1] = -x, -y, x
+        R = np.eye(3)[None] + s * K + (1.0 - c) * (K @ K)
+        return R @ self.rot0, p
+
+    def transforms(self, tick: int) -> np.ndarray:
+        """(B, 12) float32: row-major rotation then translation (the server's layout)."""
+        R, p = self.poses(tick)
+        return np.concatenate([R.reshape(-1, 9), p], axis=1).astype(np.float32)
+
+    def world(self, xf: np.ndarray) -> np.ndarray:
+        """World points of all bodies for the float32 transforms `xf`, computed exactly as
+        the server does: ((R0 x + R1 y) + R2 z) + t in float64, rounded once."""
+        body = np.repeat(np.arange(self.n_bodies), self.counts)
+        m = xf.astype(np.float64)[body]
+        p = self.local.astype(np.float64)
+        out = np.empty_like(p)
+        for r in range(3):
+            out[:, r] = ((m[:, 3 * r] * p[:, 0] + m[:, 3 * r + 1] * p[:, 1]) + m[:, 3 * r + 2] * p[:, 2]) + m[:, 9 + r]
+        return out.astype(np.float32)
+
+    def candidate_pairs(self, tick: int, n_pairs: int) -> np.ndarray:
+        """A broad-phase stand-in: the n_pairs closest body pairs by centre distance
+        (k-nearest neighbours of every body, i < j), int32 (n, 2)."""
+        from scipy.spatial import cKDTree
+        _, p = self.poses(tick)
+        k = min(self.n_bodies - 1, max(2, int(math.ceil(2.5 * n_pairs / self.n_bodies)) + 1))
+        d, j = cKDTree(p).query(p, k=k + 1)
+        i = np.repeat(np.arange(self.n_bodies), k)
+        j = j[:, 1:].reshape(-1)
+        d = d[:, 1:].reshape(-1)
+        keep = i < j
+        i, j, d = i[keep], j[keep], d[keep]
+        order = np.argsort(d, kind="stable")[:n_pairs]
+        return np.stack([i[order], j[order]], axis=1).astype(np.int32)
+
+
+def serving_scene(seed: int = 6, n_bodies: int = 20_000, lo: int = 8, hi: int = 512,
+                  half: float = 50.0, speed: float = 50.0, dt: float = 1.0 / 60.0) -> Scene:
+    """20k rigid bodies, log-uniform vertex counts in [8, 512] on random ellipsoids,
+    positions uniform in [-half, half]^3, velocities uniform in [-speed, speed]^3,
+    angular velocities up to 2 rad/s."""
+    rng = np.random.default_rng(seed)
+    counts = _loguniform_counts(rng, n_bodies, lo, hi)
+    local = _ellipsoid_points(rng, counts).astype(np.float32)
+    pos0 = rng.uniform(-half, half, size=(n_bodies, 3))
+    vel = rng.uniform(-speed, speed, size=(n_bodies, 3))
+    rot0 = _rotations(rng, n_bodies)
+    omg = _unit_vectors(rng, n_bodies) * rng.uniform(0.0, 2.0, size=(n_bodies, 1))
+    return Scene(local, counts, _offsets(counts), pos0, vel, rot0, omg, half, dt)
+
+
+def tick_sizes(seed: int, n_ticks: int, lo: int = 1_000, hi: int = 200_000) -> np.ndarray:
+    """Pairs per tick, log-uniform in [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_ticks))).astype(np.int64)
+
+
+def poisson_arrivals(seed: int, n: int, rate_hz: float) -> np.ndarray:
+    """Arrival times (s) of a Poisson process of the given rate."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate_hz, size=n))

@@ -16,6 +16,12 @@ Tolerances (stated once, used by every parity test):
     features are unique, they agree with the oracle's within ABS4 (ABS4 = 1e-4) -- for
     all but a stated small fraction: dense clouds (hundreds of points per body) make the
     contact point ill-conditioned, and the invariants above are what certify those.
+  * separated witnesses: |w1 - w0| = d within ABS4 * max(1, d), and both witnesses on
+    their bodies' supporting planes normal to the (oracle's) distance vector within ABS4;
+    where the oracle's
+    closest features are unique the witnesses agree with the oracle's within ABS4, except
+    that a pair meeting the two invariants is accepted (near-parallel closest features:
+    the closest pair is not unique to within the distance tolerance).
 """
 import numpy as np
 
@@ -134,11 +140,21 @@ def check(b, res, o, *, label="", witness_sample=2000, contact_status_bit=8):
         rep["sep_witness_length_violations"] = int(np.sum(gap > ABS4 * np.maximum(1.0, d64[sidx])))
         dirn = ow[:, 1] - ow[:, 0]
         dirn /= np.maximum(np.linalg.norm(dirn, axis=1, keepdims=True), 1e-300)
-        ok = unique_contact(b.subset(sidx), -dirn)
+        sb = b.subset(sidx)
+        ok = unique_contact(sb, -dirn)
         werr = np.abs(ws - ow).reshape(len(sidx), -1).max(axis=1)
+        # a closest pair is valid when both witnesses lie on their bodies' supporting
+        # planes normal to the distance vector (unique for convex bodies, even where the
+        # witnesses are not; the oracle's direction is used, FP32 witnesses of a small
+        # distance do not resolve it); near-parallel closest features make the pair
+        # ill-conditioned, and a valid pair is accepted there
+        ga, gb = support_gaps(sb, ws[:, 0], ws[:, 1], dirn)
+        valid = (np.abs(ga) <= ABS4) & (np.abs(gb) <= ABS4)
+        rep["sep_witness_off_support"] = int(np.sum(~valid))
         rep["sep_witness_compared"] = int(ok.sum())
         rep["sep_witness_err_max"] = float(werr[ok].max()) if ok.any() else 0.0
-        rep["sep_witness_violations"] = int(np.sum(ok & (werr > ABS4)))
+        rep["sep_witness_valid_elsewhere"] = int(np.sum(ok & (werr > ABS4) & valid))
+        rep["sep_witness_violations"] = int(np.sum(ok & (werr > ABS4) & ~valid))
     return rep
 
 
@@ -154,4 +170,5 @@ def assert_parity(rep, *, max_witness_mismatch_frac=1e-3, max_sep_witness_frac=1
     assert rep["witness_mismatch"] <= max(1, max_witness_mismatch_frac * rep["witness_compared"]), msg
     if "sep_witness_violations" in rep:
         assert rep["sep_witness_length_violations"] == 0, msg
+        assert rep["sep_witness_off_support"] == 0, msg
         assert rep["sep_witness_violations"] <= max(1, max_sep_witness_frac * rep["sep_witness_compared"]), msg

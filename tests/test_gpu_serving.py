@@ -1,0 +1,119 @@
+"""Serving loop (ogx_server_*): resident bodies, transform versions, continuous batching
+of pair requests.  Results are checked against the batch engine on the same world-space
+points and against the FP64 oracle; each request's results must be the same alone and in
+a mix of concurrent requests."""
+import numpy as np
+import pytest
+
+import parity
+from ogx import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene():
+    return W.serving_scene(seed=31, n_bodies=3000)
+
+
+def _server(scene, **kw):
+    from ogx import serving
+    return serving.Server(scene.counts, scene.local, **kw)
+
+
+def _batch(scene, world, pairs):
+    return W.Batch(world, scene.offsets, scene.counts, pairs, "serving")
+
+
+class _DeviceArray:
+    """A raw device pointer viewed as a 1-D float32 array (CUDA array interface)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f4", "data": (ptr, False), "version": 3}
+
+
+def test_world_copy_is_exact(scene):
+    """The transform kernel's world points equal the host formula bit for bit."""
+    import torch
+    from ogx import pool as P
+    with _server(scene, warm_start=False) as srv:
+        xf = scene.transforms(5)
+        v = srv.set_transforms(xf)
+        pts, _ = srv.world_layout(v)
+        packed, _ = P.pack(scene.world(xf), scene.counts)
+        torch.cuda.synchronize()
+        got = torch.as_tensor(_DeviceArray(pts, packed.shape[0]), device="cuda").cpu().numpy()
+    assert np.array_equal(got, packed)
+
+
+def test_request_matches_engine(scene, engine):
+    """Without warm starts a request gives exactly the batch engine's results on the
+    world-space points of its version."""
+    xf = scene.transforms(2)
+    pairs = scene.candidate_pairs(2, 4000)
+    with _server(scene, warm_start=False) as srv:
+        v = srv.set_transforms(xf)
+        req = srv.wait(srv.submit(v, pairs))
+    ref = engine.query(_batch(scene, scene.world(xf), pairs), engine.MODE_GJK_EPA)
+    assert np.array_equal(req.dist, ref["dist"])
+    assert np.array_equal(req.normal, ref["normal"])
+    assert np.array_equal(req.simplex["witnesses"], ref["simplex"]["witnesses"])
+    assert req.latency_ms > 0
+
+
+def test_same_alone_and_in_the_mix(scene):
+    """Continuous batching: requests admitted while others run, over more requests than
+    slots; each request's results equal its results when run alone."""
+    rng = np.random.default_rng(4)
+    ticks = [3, 4, 5, 6]
+    with _server(scene, warm_start=False, slots=2, slot_pairs=20000, max_pairs_in_flight=30000) as srv:
+        vers = {t: srv.set_transforms(scene.transforms(t)) for t in ticks}
+        jobs = []
+        for t in ticks:
+            for n in (500, 7000, 19000):
+                pairs = scene.candidate_pairs(t, n)
+                jobs.append((vers[t], pairs[rng.permutation(n)]))
+        alone = [srv.wait(srv.submit(v, p)) for v, p in jobs]
+        mixed = [srv.submit(v, p) for v, p in jobs]
+        mixed = [srv.wait(r) for r in mixed]
+    for a, m in zip(alone, mixed):
+        assert np.array_equal(a.dist, m.dist)
+        assert np.array_equal(a.normal, m.normal)
+        assert np.array_equal(a.status, m.status)
+
+
+def test_warm_start_parity(scene, orc):
+    """With warm starts (GJK starting from the previous tick's simplex) the results stay
+    within the parity tolerances of the FP64 oracle, tick after tick."""
+    with _server(scene, warm_start=True) as srv:
+        for t in (10, 11, 12):
+            xf = scene.transforms(t)
+            pairs = scene.candidate_pairs(t, 6000)
+            v = srv.set_transforms(xf)
+            req = srv.wait(srv.submit(v, pairs))
+            b = _batch(scene, scene.world(xf), pairs)
+            o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64",
+                        threads=16)
+            rep = parity.check(b, req.results(), o, label=f"tick{t}")
+            parity.assert_parity(rep, max_witness_mismatch_frac=2e-3)
+
+
+def test_admission_limits(scene):
+    from ogx import _lib
+    with _server(scene, warm_start=False, slots=1, slot_pairs=1000, max_pairs_in_flight=1000,
+                 world_slots=2) as srv:
+        v = srv.set_transforms(scene.transforms(0))
+        with pytest.raises(_lib.OgxError):
+            srv.submit(v, scene.candidate_pairs(0, 1001))
+        with pytest.raises(_lib.OgxError):
+            srv.submit(v + 1, scene.candidate_pairs(0, 10))
+        reqs = [srv.submit(v, scene.candidate_pairs(0, 900)) for _ in range(5)]
+        for r in reqs:
+            srv.wait(r)
+        assert all(np.isfinite(r.dist).all() for r in reqs)
+        # the ring holds two versions: two more updates retire version v
+        srv.set_transforms(scene.transforms(1))
+        v2 = srv.set_transforms(scene.transforms(2))
+        with pytest.raises(_lib.OgxError):
+            srv.submit(v, scene.candidate_pairs(0, 10))
+        assert srv.wait(srv.submit(v2, scene.candidate_pairs(2, 10))).dist.shape == (10,)

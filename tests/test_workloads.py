@@ -41,3 +41,27 @@ def test_pool_layout():
     assert x.tolist() == [0, 3, 6, 9, 12, 0, 0, 0]      # padding repeats point 0
     assert pool[8:16].tolist() == [1, 4, 7, 10, 13, 1, 1, 1]
     assert pool[24:28].tolist() == [1, 1, 1, 1]
+
+
+def test_serving_scene():
+    sc = W.serving_scene(seed=3, n_bodies=500)
+    assert sc.counts.min() >= 8 and sc.counts.max() <= 512
+    R, p = sc.poses(7)
+    assert np.abs(np.einsum("bij,bkj->bik", R, R) - np.eye(3)).max() < 1e-12
+    assert np.all(np.abs(p) <= sc.half + 1e-9)
+    xf = sc.transforms(7)
+    assert xf.shape == (500, 12) and xf.dtype == np.float32
+    w = sc.world(xf)
+    # the world formula in float64, one rounding
+    b = np.repeat(np.arange(500), sc.counts)
+    m = xf.astype(np.float64)[b]
+    x = sc.local.astype(np.float64)
+    ref = ((m[:, 0] * x[:, 0] + m[:, 1] * x[:, 1]) + m[:, 2] * x[:, 2]) + m[:, 9]
+    assert np.array_equal(w[:, 0], ref.astype(np.float32))
+    pairs = sc.candidate_pairs(7, 1500)
+    assert pairs.shape == (1500, 2) and np.all(pairs[:, 0] < pairs[:, 1])
+    assert len({tuple(q) for q in pairs}) == 1500
+    sizes = W.tick_sizes(1, 1000)
+    assert sizes.min() >= 1000 and sizes.max() <= 200_000
+    t = W.poisson_arrivals(1, 20000, 500.0)
+    assert abs(np.diff(t).mean() - 1 / 500.0) < 1e-4
