@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the kernel autotuner")
+    ap.add_argument("--choice", default="",
+                    help='kernel variants instead of autotuning, as printed in "kernel_choice" (JSON)')
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
@@ -313,7 +315,13 @@ def run_ours(args):
     pairs = pairs_pinned.to(f"cuda:{local}", non_blocking=True)
     out = engine.Results(n, pairs.device)
     torch.cuda.synchronize()
-    choice = ctx.autotune(pool, pairs, reps=1) if not args.no_tune else ctx.kernel_choice()
+    if args.choice:
+        for kind, row in json.loads(args.choice).items():
+            for b, (L, K) in enumerate(row):
+                ctx.set_kernel_choice(kind, b, L, K)
+        choice = ctx.kernel_choice()
+    else:
+        choice = ctx.autotune(pool, pairs, reps=1) if not args.no_tune else ctx.kernel_choice()
     torch.cuda.synchronize()
 
     # one instrumented step: per-kernel CUDA-event times and work counts
@@ -328,10 +336,12 @@ def run_ours(args):
         torch.cuda.synchronize()
         return
 
+    # the step as one CUDA graph launch (the call's launch sequence is fixed)
+    graph = engine.Graph(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
-    launches_per_step = ctx.last_launches
+            graph.launch()
+    launches_per_step = graph.kernel_launches
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -341,7 +351,7 @@ def run_ours(args):
         ev0.record(stream)
         with torch.cuda.stream(stream):
             for _ in range(args.steps):
-                engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+                graph.launch()
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
@@ -365,7 +375,7 @@ def run_ours(args):
             with torch.cuda.stream(stream):
                 pool.upload(coords_pinned)
                 pairs.copy_(pairs_pinned, non_blocking=True)
-                engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA, out=out)
+                graph.launch()
                 host_out["simplex"].copy_(out.simplex, non_blocking=True)
                 host_out["dist"].copy_(out.dist, non_blocking=True)
                 host_out["normal"].copy_(out.normal, non_blocking=True)
@@ -386,9 +396,11 @@ def run_ours(args):
             ems = float(t.item())
         e2e = {"value": world * n / (ems / 1e3), "unit": "pairs/s", "ms_per_step": ems,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "path": "ogx_pool_upload + ogx_gjk_epa + result copies, pinned host buffers"}
+               "path": "ogx_pool_upload + pair copy + ogx_graph_launch (ogx_gjk_epa) + result copies, "
+                       "pinned host buffers"}
 
     if rank != 0:
+        graph.close()
         if world > 1:
             torch.distributed.destroy_process_group()
         return
@@ -440,25 +452,28 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": spec["desc"], "pairs_per_gpu": n, "mean_vertices_per_body":
                    float(batch.counts.mean()), "l2": "inputs (pool %.2f GB) larger than L2, no flush"
-                   % (batch.coords.nbytes / 1e9), "parallelism": f"replicas x{world}"},
+                   % (batch.coords.nbytes / 1e9), "parallelism": f"replicas x{world}",
+                   "launch": f"one CUDA graph per step ({launches_per_step} kernels)"},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
         "roofline": roof,
         "kernels_ms": {k: round(v, 4) for k, v in ktimes},
         "work": counts,
         "kernel_choice": choice,
-        "autotuned": not args.no_tune,
+        "autotuned": not args.no_tune and not args.choice,
     }
     if e2e:
         line["e2e"] = e2e
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(batch)
     if not args.no_serving:
+        graph.close()
         del out, pairs
         pool.close()
         torch.cuda.empty_cache()
         line["serving"] = serving_report(local)
     print(json.dumps(line), flush=True)
+    graph.close()
     pool.close()
     ctx.close()
     if world > 1:

@@ -158,6 +158,22 @@ ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lan
 ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                         const gkCollisionPair* d_pairs, int reps);
 
+/* CUDA graph of one call: captures the launches of ogx_gjk / ogx_gjk_epa / ogx_epa
+ * (mode 1 / 2 / 3) on these buffers once; ogx_graph_launch replays them on the context's
+ * stream with one launch.  The buffers' contents may change between launches, their
+ * addresses, npairs, the kernel variants and the configuration may not (recreate the
+ * graph).  The context must have been created without a caller stream or with a
+ * non-legacy one.  A graph must be destroyed before its context. */
+typedef struct ogx_graph ogx_graph;
+ogx_status ogx_graph_create(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                            const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                            float* d_distances, float* d_normals, int32_t* d_status, int mode,
+                            ogx_graph** out);
+ogx_status ogx_graph_launch(ogx_graph* graph);
+/* kernels one replay launches */
+int ogx_graph_kernel_launches(const ogx_graph* graph);
+ogx_status ogx_graph_destroy(ogx_graph* graph);
+
 /* GJK then EPA that allocates no device memory.  No counterpart in the reference.
  * For callers that must not allocate device memory at query time: loops whose device
  * memory belongs to their own arena, real-time ticks that cannot take allocator

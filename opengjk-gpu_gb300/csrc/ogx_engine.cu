@@ -661,6 +661,80 @@ extern "C" ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int buck
   return ogx_fail(OGX_ERR_INVALID, "no variant (%d lanes, %d blocks) for bucket %d", lanes, blocks, bucket);
 }
 
+// ---------------------------------------------------------------------------------
+// CUDA graphs: the launch sequence of a call is fixed (persistent kernels, work counts on
+// the device), so one call can be captured once and replayed with one launch.
+
+struct ogx_graph {
+  ogx_ctx* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int launches = 0;
+};
+
+extern "C" ogx_status ogx_graph_create(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
+                                       const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                                       float* d_distances, float* d_normals, int32_t* d_status, int mode,
+                                       ogx_graph** out) {
+  if (!ctx || !pool || !out) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  if (mode < kModeGjk || mode > kModeEpa) return ogx_fail(OGX_ERR_INVALID, "mode %d", mode);
+  if (!ctx->stream) return ogx_fail(OGX_ERR_INVALID, "graphs need a context with its own stream");
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  // everything the call allocates is allocated before the capture
+  ogx_status s = ctx->ensure_scratch(npairs);
+  if (s) return s;
+  const bool timing = ctx->timing;
+  ctx->timing = false;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    ctx->timing = timing;
+    return ogx_cuda_fail(e, "cudaStreamBeginCapture");
+  }
+  s = ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices, d_distances,
+              d_normals, d_status, mode);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  ctx->timing = timing;
+  if (s) {
+    if (graph) cudaGraphDestroy(graph);
+    return s;
+  }
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaStreamEndCapture");
+  ogx_graph* G = new ogx_graph();
+  G->ctx = ctx;
+  G->graph = graph;
+  G->launches = ctx->last_launches;
+  e = cudaGraphInstantiate(&G->exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    delete G;
+    return ogx_cuda_fail(e, "cudaGraphInstantiate");
+  }
+  *out = G;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_graph_launch(ogx_graph* G) {
+  if (!G) return ogx_fail(OGX_ERR_INVALID, "NULL graph");
+  cudaSetDevice(G->ctx->device);
+  const cudaError_t e = cudaGraphLaunch(G->exec, G->ctx->stream);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaGraphLaunch");
+  G->ctx->last_launches = G->launches;
+  return OGX_OK;
+}
+
+extern "C" int ogx_graph_kernel_launches(const ogx_graph* G) { return G ? G->launches : 0; }
+
+extern "C" ogx_status ogx_graph_destroy(ogx_graph* G) {
+  if (!G) return OGX_OK;
+  cudaSetDevice(G->ctx->device);
+  if (G->exec) cudaGraphExecDestroy(G->exec);
+  if (G->graph) cudaGraphDestroy(G->graph);
+  delete G;
+  return OGX_OK;
+}
+
 // Times every compiled variant that can serve each bucket on the caller's batch (round r
 // runs candidate r of every bucket at once, `reps` times, keeping the best time) and keeps
 // the fastest per bucket for this context and for contexts created later on the device.

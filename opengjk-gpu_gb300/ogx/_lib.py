@@ -114,6 +114,10 @@ SIGNATURES = {
     "ogx_gjk": (_I, [_P, _P, _I, _P, _P, _P, _P]),
     "ogx_gjk_epa": (_I, [_P, _P, _I, _P, _P, _P, _P, _P]),
     "ogx_epa": (_I, [_P, _P, _I, _P, _P, _P, _P, _P]),
+    "ogx_graph_create": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P]),
+    "ogx_graph_launch": (_I, [_P]),
+    "ogx_graph_kernel_launches": (_I, [_P]),
+    "ogx_graph_destroy": (_I, [_P]),
 }
 
 _lib = None

@@ -249,6 +249,54 @@ def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Resu
     return out
 
 
+class Graph:
+    """One call captured as a CUDA graph (ogx_graph_*): `launch()` replays the whole
+    pipeline on the context's stream with one launch.  The pair and output buffers are
+    fixed at capture; their contents may change between launches."""
+
+    def __init__(self, ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Results | None = None):
+        torch = _torch()
+        assert pairs_dev.is_cuda and pairs_dev.dtype == torch.int32 and pairs_dev.is_contiguous()
+        self.ctx, self.pool, self.pairs = ctx, pool, pairs_dev
+        n = int(pairs_dev.shape[0])
+        self.out = out if out is not None else Results(n, pairs_dev.device, with_normals=(mode != MODE_GJK))
+        torch.cuda.current_stream(pairs_dev.device).synchronize()
+        P = ctypes.c_void_p
+        h = ctypes.c_void_p()
+        nrm = P(self.out.normal.data_ptr()) if self.out.normal is not None else None
+        check(ctx.lib.ogx_graph_create(ctx.handle, pool.handle, n, P(pairs_dev.data_ptr()),
+                                       P(self.out.simplex.data_ptr()), P(self.out.dist.data_ptr()), nrm,
+                                       P(self.out.status.data_ptr()), int(mode), ctypes.byref(h)))
+        self.handle = h
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.ctx.lib.ogx_graph_kernel_launches(self.handle))
+
+    def launch(self) -> Results:
+        torch = _torch()
+        cur = torch.cuda.current_stream(self.pairs.device)
+        if cur != self.ctx.stream:
+            self.ctx.stream.wait_stream(cur)
+        check(self.ctx.lib.ogx_graph_launch(self.handle))
+        if cur != self.ctx.stream:
+            cur.wait_stream(self.ctx.stream)
+        return self.out
+
+    def close(self):
+        if self.handle:
+            self.ctx.lib.ogx_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def query(batch, mode: int = MODE_GJK_EPA, config: _lib.Config | None = None, device: int = 0) -> dict:
     """One-shot convenience: upload a workloads.Batch, run, return host numpy results."""
     torch = _torch()

@@ -125,3 +125,28 @@ def test_reference_tolerance_mode(engine, orc):
     o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f32")
     diff = np.abs(res["dist"] - o["dist"])
     assert np.mean(diff <= 1e-3) > 0.995, np.mean(diff <= 1e-3)
+
+
+def test_graph_replay_matches_calls(engine):
+    """A captured call replayed as one CUDA graph launch gives the direct call's results,
+    also after the pair buffer's contents change."""
+    import torch
+    b = W.powerlaw(seed=41, n_pairs=4000)
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    pool.upload(b.coords)
+    pairs = torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()
+    ref = engine.run(ctx, pool, pairs, engine.MODE_GJK_EPA).to_host()
+    g = engine.Graph(ctx, pool, pairs, engine.MODE_GJK_EPA)
+    assert g.kernel_launches == ctx.last_launches
+    for _ in range(2):
+        got = g.launch().to_host()
+        ctx.synchronize()
+        assert np.array_equal(got["dist"], ref["dist"]) and np.array_equal(got["normal"], ref["normal"])
+    flipped = pairs.flip(0).contiguous()
+    pairs.copy_(flipped)
+    ref2 = engine.run(ctx, pool, flipped, engine.MODE_GJK_EPA).to_host()
+    got2 = g.launch().to_host()
+    ctx.synchronize()
+    assert np.array_equal(got2["dist"], ref2["dist"])
+    g.close()
