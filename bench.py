@@ -213,6 +213,40 @@ def serving_report(device: int, seed: int = 77) -> dict:
         lat_mix, thr_mix = run(list(range(n_lists)), mix_rate, 300, seed + 1)
         big_rate = 0.5 * cap_big_hz
         lat_big, thr_big = run(big, big_rate, 100, seed + 2)
+
+        # phase 3: the pairs come from the device broad phase (boxes grown by one tick of
+        # the fastest motion, 50 * dt), GJK + EPA on them, nothing on the host in between
+        cell, margin = 5.0, 50.0 * scene.dt
+
+        def broad_burst(n):
+            t0 = time.perf_counter()
+            reqs = [srv.submit_broadphase(srv.set_transforms(xfs[k % n_lists]), cell, margin) for k in range(n)]
+            for r in reqs:
+                srv.wait(r)
+            return time.perf_counter() - t0, reqs
+        broad_burst(n_lists)
+        dtb, reqs = broad_burst(n_lists)
+        found = [int(r.count[0]) for r in reqs]
+        cap_broad_hz = n_lists / dtb
+        broad_rate = 0.5 * cap_broad_hz
+        arrivals = W.poisson_arrivals(seed + 3, 200, broad_rate)
+        outb = [None] * len(arrivals)
+        t0 = time.perf_counter() + 0.05
+
+        def submitter_b():
+            for k in range(len(arrivals)):
+                while time.perf_counter() < t0 + arrivals[k]:
+                    time.sleep(5e-5)
+                outb[k] = srv.submit_broadphase(srv.set_transforms(xfs[k % n_lists]), cell, margin)
+        thr = th.Thread(target=submitter_b)
+        thr.start()
+        lat_b = []
+        for k in range(len(arrivals)):
+            while outb[k] is None:
+                time.sleep(5e-5)
+            lat_b.append(srv.wait(outb[k]).latency_ms)
+        thr.join()
+        lat_b = np.array(lat_b)
     finally:
         srv.close()
     return {
@@ -224,6 +258,10 @@ def serving_report(device: int, seed: int = 77) -> dict:
                   "p50_ms": float(np.percentile(lat_mix, 50)), "p99_ms": float(np.percentile(lat_mix, 99))},
         "ticks_200k": {"rate_hz": big_rate, "ticks": len(lat_big), "pairs_per_s": thr_big,
                        "p50_ms": float(np.percentile(lat_big, 50)), "p99_ms": float(np.percentile(lat_big, 99))},
+        "broadphase_ticks": {"rate_hz": broad_rate, "ticks": len(lat_b), "cell": cell, "margin": margin,
+                             "mean_pairs_per_tick": float(np.mean(found)),
+                             "capacity_ticks_per_s": cap_broad_hz,
+                             "p50_ms": float(np.percentile(lat_b, 50)), "p99_ms": float(np.percentile(lat_b, 99))},
         "latency": "submit -> results in host memory, host clock",
     }
 

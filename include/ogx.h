@@ -62,6 +62,10 @@ typedef struct ogx_config {
 #define OGX_FLAG_FP64_ESCALATE 1 /* near-degenerate steps re-run in FP64 */
 #define OGX_FLAG_FP64_POLISH 2   /* final simplex / EPA face re-solved in FP64 */
 #define OGX_FLAG_REFERENCE_TOL 4 /* reference termination rules */
+#define OGX_FLAG_EPA_FP64_PLANES 8 /* every EPA face plane solved in FP64 (the engine
+                                    * turns this on itself for contacts whose FP32
+                                    * expansion ran out of room or met an inconsistent
+                                    * horizon: they are run again from the start) */
 
 /* Per-pair status bits (optional output of the engine API). */
 #define OGX_PAIR_GJK_CAP 1
@@ -158,6 +162,22 @@ ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lan
 ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                         const gkCollisionPair* d_pairs, int reps);
 
+/* Device broad phase (uniform grid): every pair i < j of a pool's bodies whose
+ * axis-aligned boxes, each grown by `margin`, overlap - exactly once, sorted by (i, j).
+ * The pairs feed the GJK/EPA calls directly (d_pairs).  `cell` is the grid cell size:
+ * any positive value gives the same pairs, a cell near the largest box extent the least
+ * work; a box may touch at most 64 cells.  Writes min(count, max_pairs) pairs and
+ * d_result[0] = count (all overlapping pairs, may exceed max_pairs), d_result[1] = error
+ * flags (1: a box beyond 2^20 cells from the origin, 2: a box touching more than 64
+ * cells; such bodies get no pairs).  Asynchronous on the context's stream.
+ * Replaces the per-frame grid of the reference's visualiser
+ * (visualization/integrate_final_gjk.cu:467-570, 916-1002). */
+typedef struct ogx_broad ogx_broad;
+ogx_status ogx_broad_create(ogx_ctx* ctx, int max_bodies, ogx_broad** out);
+ogx_status ogx_broadphase(ogx_broad* broad, const ogx_pool* pool, float cell, float margin,
+                          int max_pairs, gkCollisionPair* d_pairs, int* d_result);
+ogx_status ogx_broad_destroy(ogx_broad* broad);
+
 /* CUDA graph of one call: captures the launches of ogx_gjk / ogx_gjk_epa / ogx_epa
  * (mode 1 / 2 / 3) on these buffers once; ogx_graph_launch replays them on the context's
  * stream with one launch.  The buffers' contents may change between launches, their
@@ -232,6 +252,15 @@ ogx_status ogx_server_set_transforms(ogx_server* server, const float* xf, int64_
 ogx_status ogx_server_submit(ogx_server* server, int64_t version, int npairs,
                              const gkCollisionPair* pairs, gkSimplex* simplices,
                              float* distances, float* normals, int32_t* status, int64_t* ticket);
+/* Queue a broad-phase request: the pairs are every pair of bodies whose boxes (grown by
+ * margin) overlap in the version's world copy (ogx_broadphase on the device), then
+ * GJK + EPA on them, all on the device.  pairs[max_pairs] receives the pairs (sorted,
+ * i < j), count[0] the number found (may exceed max_pairs; the first
+ * min(count, max_pairs, slot_pairs) are run), count[1] the broad phase's error flags. */
+ogx_status ogx_server_submit_broadphase(ogx_server* server, int64_t version, float cell,
+                                        float margin, int max_pairs, gkCollisionPair* pairs,
+                                        int32_t* count, gkSimplex* simplices, float* distances,
+                                        float* normals, int32_t* status, int64_t* ticket);
 ogx_status ogx_server_poll(ogx_server* server, int64_t ticket, int* done);
 /* Wait for a request (timeout_s <= 0: no limit); latency_ms = completion - submission
  * on the host clock.  The ticket is released. */

@@ -1,0 +1,350 @@
+// ogx_broad.cu -- device broad phase: candidate pairs from the bodies' boxes on a uniform
+// grid, the producer of the narrow phase's pair lists.
+//
+// The reference's visualiser builds its per-frame pairs with a uniform grid (count / scan
+// / generate, visualization/integrate_final_gjk.cu:467-570 and 916-1002, with the scan of
+// visualization/utils/scan_kernels.cuh:194) and copies counts to the host between steps.
+// Here everything stays on the device and the output is deterministic:
+//   1. k_box       axis-aligned box of every body (min / max over its points), grown by a
+//                  margin, and the number of grid cells it touches;
+//   2. scan        cell entries per body -> entry offsets;
+//   3. k_entries   one entry (cell key, body) per touched cell, counted per hash bucket;
+//   4. scan        bucket counts -> bucket offsets; k_scatter groups entries by bucket;
+//   5. k_pairs     per body i: every body j > i sharing one of i's cells whose box
+//                  overlaps i's box, emitted only in the cell holding the low corner of
+//                  the two boxes' intersection (so once); pass 1 counts, a scan gives
+//                  each body its output range, pass 2 writes and sorts the range by j.
+// The result is every overlapping pair (i < j) exactly once, sorted by (i, j),
+// whatever the grid resolution; the cell size only changes the work.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "ogx_engine.h"
+
+using namespace ogx;
+
+namespace {
+
+constexpr int kMaxCellsPerBody = 64;
+constexpr int kAxisBits = 21;                  // cell coordinates in (-2^20, 2^20)
+constexpr int kAxisBias = 1 << (kAxisBits - 1);
+
+__device__ __forceinline__ uint64_t cell_key(int x, int y, int z) {
+  const uint64_t m = (1ull << kAxisBits) - 1ull;
+  return ((uint64_t)(x + kAxisBias) & m) | (((uint64_t)(y + kAxisBias) & m) << kAxisBits) |
+         (((uint64_t)(z + kAxisBias) & m) << (2 * kAxisBits));
+}
+
+__device__ __forceinline__ uint32_t key_hash(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  return (uint32_t)k;
+}
+
+__device__ __forceinline__ int cell_of(float x, float inv) { return (int)floorf(x * inv); }
+
+// flags in the error word
+enum { kErrCellRange = 1, kErrCellsPerBody = 2 };
+
+__global__ void k_box(const float* __restrict__ pool, const BodyRef* __restrict__ bodies, int n, float margin,
+                      float inv_cell, float4* __restrict__ lo, float4* __restrict__ hi, int* __restrict__ ncells,
+                      int* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int b = warp; b < n; b += nwarps) {
+    const BodyRef r = bodies[b];
+    const int n4 = round4(r.n);
+    const float* X = pool + 4 * (size_t)r.quad;
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = lane; i < r.n; i += 32)
+      for (int c = 0; c < 3; ++c) {
+        const float v = X[c * n4 + i];
+        mn[c] = fminf(mn[c], v);
+        mx[c] = fmaxf(mx[c], v);
+      }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int c = 0; c < 3; ++c) {
+        mn[c] = fminf(mn[c], __shfl_xor_sync(0xffffffffu, mn[c], o));
+        mx[c] = fmaxf(mx[c], __shfl_xor_sync(0xffffffffu, mx[c], o));
+      }
+    if (lane == 0) {
+      const float4 l = make_float4(mn[0] - margin, mn[1] - margin, mn[2] - margin, 0.0f);
+      const float4 h = make_float4(mx[0] + margin, mx[1] + margin, mx[2] + margin, 0.0f);
+      lo[b] = l;
+      hi[b] = h;
+      long long cnt = 1;
+      bool bad = false;
+      const float ll[3] = {l.x, l.y, l.z}, hh[3] = {h.x, h.y, h.z};
+      for (int c = 0; c < 3; ++c) {
+        const int a = cell_of(ll[c], inv_cell), z = cell_of(hh[c], inv_cell);
+        bad |= !(a > -kAxisBias && z < kAxisBias);
+        cnt *= (long long)(z - a + 1);
+      }
+      if (bad) atomicOr(err, kErrCellRange);
+      if (cnt > kMaxCellsPerBody) atomicOr(err, kErrCellsPerBody);
+      ncells[b] = (bad || cnt > kMaxCellsPerBody) ? 0 : (int)cnt;
+    }
+  }
+}
+
+// exclusive scan of n ints in place: tiles of 1024 (one block each) are reduced, the
+// tile sums scanned by one block, then every tile scanned with its offset
+constexpr int kTile = 1024;
+
+__device__ __forceinline__ int block_incl_scan(int x, int* warp_sums) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int t = warp_sums[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    warp_sums[lane] = t;
+  }
+  __syncthreads();
+  return x + (w > 0 ? warp_sums[w - 1] : 0);
+}
+
+__global__ void __launch_bounds__(kTile) k_tile_sums(const int* __restrict__ a, int n, int* __restrict__ sums) {
+  __shared__ int ws[32];
+  const int i = blockIdx.x * kTile + threadIdx.x;
+  const int inc = block_incl_scan(i < n ? a[i] : 0, ws);
+  if (threadIdx.x == kTile - 1) sums[blockIdx.x] = inc;
+}
+
+// one block: exclusive scan of the tile sums (at most kTile * kTile elements overall)
+__global__ void __launch_bounds__(kTile) k_scan_sums(int* __restrict__ sums, int ntiles, int* __restrict__ total) {
+  __shared__ int ws[32];
+  const int x = threadIdx.x < ntiles ? sums[threadIdx.x] : 0;
+  const int inc = block_incl_scan(x, ws);
+  if (threadIdx.x < ntiles) sums[threadIdx.x] = inc - x;
+  if (threadIdx.x == kTile - 1 && total) *total = inc;
+}
+
+__global__ void __launch_bounds__(kTile) k_tile_scan(int* __restrict__ a, int n, const int* __restrict__ sums) {
+  __shared__ int ws[32];
+  const int i = blockIdx.x * kTile + threadIdx.x;
+  const int x = i < n ? a[i] : 0;
+  const int inc = block_incl_scan(x, ws);
+  if (i < n) a[i] = sums[blockIdx.x] + inc - x;
+}
+
+__global__ void k_entries(const float4* __restrict__ lo, const float4* __restrict__ hi, int n, float inv_cell,
+                          const int* __restrict__ eoff, unsigned long long* __restrict__ ekey,
+                          int* __restrict__ ebody, uint32_t bmask, int* __restrict__ bcount) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+    const int e0 = eoff[b], e1 = eoff[b + 1];
+    if (e1 == e0) continue;
+    const float4 l = lo[b], h = hi[b];
+    const int x0 = cell_of(l.x, inv_cell), x1 = cell_of(h.x, inv_cell);
+    const int y0 = cell_of(l.y, inv_cell), y1 = cell_of(h.y, inv_cell);
+    const int z0 = cell_of(l.z, inv_cell), z1 = cell_of(h.z, inv_cell);
+    int e = e0;
+    for (int x = x0; x <= x1; ++x)
+      for (int y = y0; y <= y1; ++y)
+        for (int z = z0; z <= z1; ++z) {
+          const uint64_t k = cell_key(x, y, z);
+          ekey[e] = k;
+          ebody[e] = b;
+          atomicAdd(bcount + (key_hash(k) & bmask), 1);
+          ++e;
+        }
+  }
+}
+
+__global__ void k_scatter(const unsigned long long* __restrict__ ekey, const int* __restrict__ ebody,
+                          const int* __restrict__ ne_dev, uint32_t bmask, int* __restrict__ bcursor,
+                          unsigned long long* __restrict__ skey, int* __restrict__ sbody) {
+  const int ne = *ne_dev;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+    const uint64_t k = ekey[e];
+    const int s = atomicAdd(bcursor + (key_hash(k) & bmask), 1);
+    skey[s] = k;
+    sbody[s] = ebody[e];
+  }
+}
+
+// pass 0 counts the pairs of every body, pass 1 writes them at off[i] and sorts by j
+template <int PASS>
+__global__ void k_pairs(const float4* __restrict__ lo, const float4* __restrict__ hi, int n, float inv_cell,
+                        const int* __restrict__ eoff, const unsigned long long* __restrict__ ekey,
+                        uint32_t bmask, const int* __restrict__ boff, const int* __restrict__ bend,
+                        const unsigned long long* __restrict__ skey, const int* __restrict__ sbody,
+                        int* __restrict__ pcount, int2* __restrict__ out, int cap) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 li = lo[i], hi_ = hi[i];
+    int cnt = 0;
+    const int base = PASS == 1 ? pcount[i] : 0;
+    for (int e = eoff[i]; e < eoff[i + 1]; ++e) {
+      const uint64_t k = ekey[e];
+      const uint32_t h = key_hash(k) & bmask;
+      for (int s = boff[h]; s < bend[h]; ++s) {
+        if (skey[s] != k) continue;
+        const int j = sbody[s];
+        if (j <= i) continue;
+        const float4 lj = lo[j], hj = hi[j];
+        const float mx = fmaxf(li.x, lj.x), my = fmaxf(li.y, lj.y), mz = fmaxf(li.z, lj.z);
+        if (mx > fminf(hi_.x, hj.x) || my > fminf(hi_.y, hj.y) || mz > fminf(hi_.z, hj.z)) continue;
+        if (cell_key(cell_of(mx, inv_cell), cell_of(my, inv_cell), cell_of(mz, inv_cell)) != k) continue;
+        if (PASS == 1 && base + cnt < cap) out[base + cnt] = make_int2(i, j);
+        ++cnt;
+      }
+    }
+    if (PASS == 0) {
+      pcount[i] = cnt;
+    } else {
+      // sort this body's range by j (insertion sort: ranges are short)
+      const int m = min(cnt, cap - base);
+      for (int a = 1; a < m; ++a) {
+        const int2 v = out[base + a];
+        int b = a - 1;
+        while (b >= 0 && out[base + b].y > v.y) {
+          out[base + b + 1] = out[base + b];
+          --b;
+        }
+        out[base + b + 1] = v;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+struct ogx_broad {
+  ogx_ctx* ctx = nullptr;
+  int max_bodies = 0;
+  uint32_t nbuckets = 0;
+  float4 *lo = nullptr, *hi = nullptr;
+  int* eoff = nullptr;        // max_bodies + 1
+  unsigned long long* ekey = nullptr;
+  int* ebody = nullptr;       // max_bodies * kMaxCellsPerBody entries
+  unsigned long long* skey = nullptr;
+  int* sbody = nullptr;
+  int* boff = nullptr;        // nbuckets
+  int* bend = nullptr;        // nbuckets
+  int* pcount = nullptr;      // max_bodies + 1
+  int* scal = nullptr;        // [0] entries, [1] pairs, [2] error flags
+  int* tiles = nullptr;       // tile sums of the scans
+};
+
+// exclusive scan of a[0..n) on the stream; *total = the sum (may be null)
+cudaError_t scan(ogx_broad* B, int* a, int n, int* total, cudaStream_t st) {
+  const int ntiles = (n + kTile - 1) / kTile;
+  if (ntiles > kTile) return cudaErrorInvalidValue;
+  k_tile_sums<<<ntiles, kTile, 0, st>>>(a, n, B->tiles);
+  k_scan_sums<<<1, kTile, 0, st>>>(B->tiles, ntiles, total);
+  k_tile_scan<<<ntiles, kTile, 0, st>>>(a, n, B->tiles);
+  return cudaGetLastError();
+}
+
+extern "C" ogx_status ogx_broad_create(ogx_ctx* ctx, int max_bodies, ogx_broad** out) {
+  if (!ctx || !out || max_bodies < 1) return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  ogx_broad* B = new ogx_broad();
+  B->ctx = ctx;
+  B->max_bodies = max_bodies;
+  // about two buckets per expected entry (a body touches ~4-8 cells at a sensible cell
+  // size); the scans take at most kTile * kTile elements
+  uint32_t nb = 1024;
+  while (nb < 8u * (uint32_t)max_bodies && nb < (uint32_t)(kTile * kTile)) nb <<= 1;
+  if ((size_t)max_bodies + 1 > (size_t)kTile * kTile)
+    return ogx_fail(OGX_ERR_CAPACITY, "broad phase takes at most %d bodies", kTile * kTile - 1);
+  B->nbuckets = nb;
+  const size_t ne = (size_t)max_bodies * kMaxCellsPerBody;
+  cudaError_t e;
+  if ((e = cudaMalloc(&B->lo, max_bodies * sizeof(float4))) != cudaSuccess ||
+      (e = cudaMalloc(&B->hi, max_bodies * sizeof(float4))) != cudaSuccess ||
+      (e = cudaMalloc(&B->eoff, (max_bodies + 1) * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->ekey, ne * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&B->ebody, ne * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->skey, ne * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&B->sbody, ne * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->boff, nb * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->bend, nb * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->pcount, (max_bodies + 1) * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->scal, 4 * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&B->tiles, kTile * sizeof(int))) != cudaSuccess) {
+    ogx_broad_destroy(B);
+    return ogx_cuda_fail(e, "broad-phase allocation");
+  }
+  *out = B;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_broad_destroy(ogx_broad* B) {
+  if (!B) return OGX_OK;
+  cudaSetDevice(B->ctx->device);
+  cudaFree(B->lo);
+  cudaFree(B->hi);
+  cudaFree(B->eoff);
+  cudaFree(B->ekey);
+  cudaFree(B->ebody);
+  cudaFree(B->skey);
+  cudaFree(B->sbody);
+  cudaFree(B->boff);
+  cudaFree(B->bend);
+  cudaFree(B->pcount);
+  cudaFree(B->scal);
+  cudaFree(B->tiles);
+  delete B;
+  return OGX_OK;
+}
+
+ogx_status broad_run(ogx_broad* B, cudaStream_t st, const float* d_points, const BodyRef* d_bodies, int nbodies,
+                     float cell, float margin, int max_pairs, gkCollisionPair* d_pairs, int* d_result) {
+  if (nbodies > B->max_bodies) return ogx_fail(OGX_ERR_CAPACITY, "%d bodies > broad-phase capacity %d", nbodies,
+                                               B->max_bodies);
+  if (!(cell > 0.0f) || !(margin >= 0.0f) || max_pairs < 0 || !d_result)
+    return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
+  const int sms = B->ctx->sm_count;
+  const float inv = 1.0f / cell;
+  const uint32_t bmask = B->nbuckets - 1u;
+  cudaError_t e = cudaMemsetAsync(B->scal, 0, 4 * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->boff, 0, B->nbuckets * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->eoff + nbodies, 0, sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->pcount + nbodies, 0, sizeof(int), st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "broad-phase reset");
+  const int gw = std::max(1, std::min(8 * sms, (nbodies + 3) / 4));
+  k_box<<<gw, 128, 0, st>>>(d_points, d_bodies, nbodies, margin, inv, B->lo, B->hi, B->eoff, B->scal + 2);
+  e = scan(B, B->eoff, nbodies + 1, B->scal + 0, st);
+  const int gb = std::max(1, std::min(8 * sms, (nbodies + 127) / 128));
+  if (e == cudaSuccess) {
+    k_entries<<<gb, 128, 0, st>>>(B->lo, B->hi, nbodies, inv, B->eoff, B->ekey, B->ebody, bmask, B->boff);
+    e = scan(B, B->boff, (int)B->nbuckets, nullptr, st);
+  }
+  // the scatter advances a copy of the bucket offsets, leaving it at the buckets' ends
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(B->bend, B->boff, B->nbuckets * sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) {
+    k_scatter<<<8 * sms, 256, 0, st>>>(B->ekey, B->ebody, B->scal + 0, bmask, B->bend, B->skey, B->sbody);
+    k_pairs<0><<<gb, 128, 0, st>>>(B->lo, B->hi, nbodies, inv, B->eoff, B->ekey, bmask, B->boff, B->bend,
+                                   B->skey, B->sbody, B->pcount, nullptr, 0);
+    e = scan(B, B->pcount, nbodies + 1, B->scal + 1, st);
+  }
+  if (e == cudaSuccess)
+    k_pairs<1><<<gb, 128, 0, st>>>(B->lo, B->hi, nbodies, inv, B->eoff, B->ekey, bmask, B->boff, B->bend,
+                                   B->skey, B->sbody, B->pcount, reinterpret_cast<int2*>(d_pairs), max_pairs);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "broad-phase launch");
+  e = cudaMemcpyAsync(d_result, B->scal + 1, 2 * sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "broad-phase launch");
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_broadphase(ogx_broad* B, const ogx_pool* pool, float cell, float margin, int max_pairs,
+                                     gkCollisionPair* d_pairs, int* d_result) {
+  if (!B || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL broad phase or pool");
+  cudaSetDevice(B->ctx->device);
+  return broad_run(B, B->ctx->stream, pool->d_points, pool->d_bodies, pool->nbodies, cell, margin, max_pairs,
+                   d_pairs, d_result);
+}

@@ -128,6 +128,7 @@ enum {
   OGX_F_FP64_ESCALATE = OGX_FLAG_FP64_ESCALATE,  // near-degenerate steps re-run in FP64
   OGX_F_FP64_POLISH = OGX_FLAG_FP64_POLISH,      // final simplex / face re-solved in FP64
   OGX_F_REFERENCE_TOL = OGX_FLAG_REFERENCE_TOL,  // reference termination rules
+  OGX_F_EPA_FP64_PLANES = OGX_FLAG_EPA_FP64_PLANES,  // every EPA face plane from FP64
 };
 
 // Per-pair status bits written beside the results.

@@ -108,7 +108,7 @@ bool g_tuned_valid[16];
 
 // can variant v serve bucket b?
 bool serves(const Launch& v, int b) {
-  if (v.K == 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
+  if (v.K <= 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
   if (b == kBuckets - 1) return false;
   const int cap = 4 * v.L * v.K;
   return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];

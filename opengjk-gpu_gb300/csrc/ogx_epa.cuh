@@ -82,7 +82,7 @@ OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
 
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
 template <class Mem, class Bodies>
-OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, bool escalate,
+OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, bool escalate, bool all64,
                          int& status) {
   const float4 P0 = M.vp[a], P1 = M.vp[b], P2 = M.vp[c];
   const fv3 p0 = v3<float>(P0.x, P0.y, P0.z);
@@ -92,7 +92,7 @@ OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, boo
   const float nn = dot(n, n);
   const float s = l1(e0) * l1(e1);
   float4 r;
-  if (escalate && nn < 1e-6f * s * s) {
+  if (all64 || (escalate && nn < 1e-6f * s * s)) {
     // sine of the face angle below ~1e-3: FP32 normal unreliable
     const dv3 q0 = B.dpoint(0, M.vid[a].x) - B.dpoint(1, M.vid[a].y);
     const dv3 q1 = B.dpoint(0, M.vid[b].x) - B.dpoint(1, M.vid[b].y);
@@ -289,6 +289,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   const int L = Team::L;
   const int lane = t.lane();
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
+  const bool all64 = (cfg.flags & OGX_F_EPA_FP64_PLANES) != 0;
   o.status = 0;
   o.iters = 0;
   o.polish = false;
@@ -402,7 +403,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     M.fa[f][0] = (uint8_t)(f == 0 ? 3 : 0);
     M.fa[f][1] = (uint8_t)(f == 0 || f == 1 ? 2 : (f == 2 ? 3 : 1));
     M.fa[f][2] = (uint8_t)(f == 0 ? 1 : (f == 1 ? 3 : (f == 2 ? 1 : 2)));
-    const float4 pl = face_plane(M, B, va, vb, vc, escalate, st);
+    const float4 pl = face_plane(M, B, va, vb, vc, escalate, all64, st);
     M.fn[f] = pl;
     if (pl.w < cbd) {
       cbd = pl.w;
@@ -489,8 +490,13 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       nvis += popc32(m);
     }
     t.sync();
-    // the closest face must be seen (gain >= tol > vis threshold); otherwise stop
+    // the closest face must be seen (gain >= tol > vis threshold); otherwise stop (or,
+    // from the small pass, start again with FP64 planes in the full pass)
     if (!M.vis[best]) {
+      if (can_spill && escalate) {
+        o.spill = true;
+        return;
+      }
       o.status |= OGX_S_EPA_TOPOLOGY;
       done = true;
       break;
@@ -521,6 +527,10 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     }
     // new face k goes to vlist[k] (k < nvis), else to fresh slot fend + k - nvis
     if (htot < 3) {
+      if (can_spill && escalate) {
+        o.spill = true;
+        return;
+      }
       o.status |= OGX_S_EPA_TOPOLOGY;
       done = true;
       break;
@@ -555,6 +565,10 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       bad |= (M.hstart[M.hz[k][0]] != s) || (M.hend[M.hz[k][1]] != s);
     }
     if (t.any(bad)) {
+      if (can_spill && escalate) {
+        o.spill = true;
+        return;
+      }
       o.status |= OGX_S_EPA_TOPOLOGY;
       done = true;
       break;
@@ -569,7 +583,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       M.fa[s][0] = M.hz[k][2];
       M.fa[s][1] = M.hstart[b];
       M.fa[s][2] = M.hend[a];
-      const float4 pl = face_plane(M, B, a, b, p, escalate, st);
+      const float4 pl = face_plane(M, B, a, b, p, escalate, all64, st);
       M.fn[s] = pl;
       M.fv[s][3] = 1;
       if (pl.w < cbd || (pl.w == cbd && s < cbest)) {

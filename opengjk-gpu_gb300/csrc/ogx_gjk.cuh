@@ -524,36 +524,65 @@ OGX_HD int escalate_step(const MemBodies B, int n, const int* ia, const int* ib,
   return sd.n;
 }
 
-template <class Team, class Bodies>
-OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g, int start_a = 0,
-                     int start_b = 0) {
-  const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
-  const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
+// GJK as a resumable loop: gjk_start sets the state up, each gjk_iterate runs one
+// iteration (support, termination tests, sub-distance step) until r.done, gjk_end
+// finishes (witnesses, certification).  gjk_pair chains them; the interleaved kernels
+// run one iteration of a different pair in every lane.
+struct GjkRun {
+  fv3 v;
+  fv3 P[4];  // simplex in registers: slots 0..3, newest last; every index is unrolled
+  int IA[4], IB[4];
+  int n;
+  float wmax2;
+  fv3 sa, sb;
+  int ia, ib;
+  int k;
+  int status, exit;
+  bool done;
+};
+
+template <class Bodies>
+OGX_HD void gjk_start(const Bodies& B, GjkRun& r, int start_a = 0, int start_b = 0) {
   // first point of the Minkowski difference: point 0 of each body (the reference's
   // start), or a warm-start pair of vertex indices (e.g. the previous frame's simplex)
-  const int ia0 = start_a, ib0 = start_b;
-  const fv3 a0 = B.point(0, ia0), b0 = B.point(1, ib0);
-  fv3 v = a0 - b0;
-  // simplex in registers: slots 0..3, newest last; every index below is unrolled
-  fv3 P[4];
-  int IA[4], IB[4];
-  P[0] = v;
-  P[1] = P[2] = P[3] = v;
-  IA[0] = ia0;
-  IB[0] = ib0;
-  IA[1] = IA[2] = IA[3] = IB[1] = IB[2] = IB[3] = -1;
-  int n = 1;
-  g.status = 0;
-  g.exit = 0;
-  float wmax2 = 0.0f;
-  fv3 sa = a0, sb = b0;
-  int ia = ia0, ib = ib0;
+  const fv3 a0 = B.point(0, start_a), b0 = B.point(1, start_b);
+  r.v = a0 - b0;
+  r.P[0] = r.v;
+  r.P[1] = r.P[2] = r.P[3] = r.v;
+  r.IA[0] = start_a;
+  r.IB[0] = start_b;
+  r.IA[1] = r.IA[2] = r.IA[3] = r.IB[1] = r.IB[2] = r.IB[3] = -1;
+  r.n = 1;
+  r.wmax2 = 0.0f;
+  r.sa = a0;
+  r.sb = b0;
+  r.ia = start_a;
+  r.ib = start_b;
+  r.k = 0;
+  r.status = 0;
+  r.exit = 0;
+  r.done = false;
+}
+
+template <class Team, class Bodies>
+OGX_HD void gjk_iterate(const Team& t, const Bodies& B, const Config& cfg, GjkRun& r) {
+  const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
+  const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
   const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
   // |v| this small against the simplex points is below FP32 resolution: stop
   const float contact = reftol ? cfg.gjk_eps_tot : 0.5f * FLT_EPSILON;
-  int k = 0;
-  for (;;) {
-    ++k;
+  fv3& v = r.v;
+  fv3* P = r.P;
+  int* IA = r.IA;
+  int* IB = r.IB;
+  int& n = r.n;
+  float& wmax2 = r.wmax2;
+  fv3& sa = r.sa;
+  fv3& sb = r.sb;
+  int& ia = r.ia;
+  int& ib = r.ib;
+  int& k = r.k;
+  ++k;
     const fv3 mv = -v;
     float ba, bb;
     int xa, xb;
@@ -578,24 +607,28 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
       floor_ = fmaxf(floor_, cfg.gjk_noise * FLT_EPSILON * nv * (nv + sqrtf(dot(w, w))));
     }
     if (gap <= cfg.gjk_eps_rel * vv) {
-      g.exit = GJK_EXIT_GAP_REL;
-      break;
+      r.exit = GJK_EXIT_GAP_REL;
+      r.done = true;
+      return;
     }
     if (gap < floor_) {
-      g.exit = GJK_EXIT_GAP_NOISE;
-      break;
+      r.exit = GJK_EXIT_GAP_NOISE;
+      r.done = true;
+      return;
     }
     if (vv < eps_rel2) {
-      g.exit = GJK_EXIT_NULL_V;
-      break;
+      r.exit = GJK_EXIT_NULL_V;
+      r.done = true;
+      return;
     }
     if (!reftol) {
       bool dup = false;
 #pragma unroll
       for (int j = 0; j < 4; ++j) dup |= (j < n) && IA[j] == ia && IB[j] == ib;
       if (dup) {
-        g.exit = GJK_EXIT_DUPLICATE;
-        break;
+        r.exit = GJK_EXIT_DUPLICATE;
+        r.done = true;
+        return;
       }
     }
 #pragma unroll
@@ -638,7 +671,7 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
       fv3 vd;
       nn = escalate_step(B.mem_view(), n, ias, ibs, v, order, &vd);
       v = vd;
-      g.status |= OGX_S_GJK_ESCALATED;
+      r.status |= OGX_S_GJK_ESCALATED;
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         const int sj = order[j];
@@ -671,18 +704,34 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
     for (int j = 0; j < 4; ++j)
       if (j < n) wmax2 = fmaxf(wmax2, dot(P[j], P[j]));
     if (dot(v, v) <= contact * contact * wmax2) {
-      g.exit = GJK_EXIT_CONTACT;
-      break;
+      r.exit = GJK_EXIT_CONTACT;
+      r.done = true;
+      return;
     }
     if (n == 4) {
-      g.exit = GJK_EXIT_ENCLOSED;
-      break;
+      r.exit = GJK_EXIT_ENCLOSED;
+      r.done = true;
+      return;
     }
     if (k == cfg.gjk_max_iter) {
-      g.exit = GJK_EXIT_CAP;
-      break;
+      r.exit = GJK_EXIT_CAP;
+      r.done = true;
+      return;
     }
-  }
+}
+
+template <class Team, class Bodies>
+OGX_HD void gjk_end(const Team& t, const Bodies& B, const Config& cfg, const GjkRun& r, GjkState& g) {
+  const fv3 v = r.v;
+  const fv3* P = r.P;
+  const int* IA = r.IA;
+  const int* IB = r.IB;
+  const int n = r.n;
+  const float wmax2 = r.wmax2;
+  const int ia = r.ia, ib = r.ib;
+  const int k = r.k;
+  g.status = r.status;
+  g.exit = r.exit;
   g.n = n;
   g.wmax2 = wmax2;
 #pragma unroll
@@ -747,6 +796,15 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
     const float eb = 4.0f * FLT_EPSILON * bm * l1v + bm * dv;
     g.certain = (a1 - ao > 2.0f * ea) && (b1 - bo > 2.0f * eb);
   }
+}
+
+template <class Team, class Bodies>
+OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g, int start_a = 0,
+                     int start_b = 0) {
+  GjkRun r;
+  gjk_start(B, r, start_a, start_b);
+  while (!r.done) gjk_iterate(t, B, cfg, r);
+  gjk_end(t, B, cfg, r, g);
 }
 
 // Exact (FP64) support index of body w along d.  An FP32 scan finds the maximum m of
@@ -864,7 +922,7 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
     gap = fmin(gap, dot(r.v, e));
     dmax = fmax(dmax, dot(e, e));
   }
-  const double floor64 = 64.0 * DBL_EPSILON * sqrt(r.wmax2) * sqrt(dmax);
+  const double floor64 = 4.0 * DBL_EPSILON * sqrt(r.wmax2) * sqrt(dmax);
   if (gap <= 1e-12 * vv || gap <= floor64) {
     r.done = true;
     return;

@@ -260,8 +260,8 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// EPA at full capacity (EpaMem) over the spill list: one warp per contact, points read
-// from memory (any body size)
+// EPA at full capacity (EpaMem) over the spill list, every face plane from FP64: one warp
+// per contact, points read from memory (any body size)
 __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMem* mem = reinterpret_cast<EpaMem*>(smem_raw);
@@ -270,8 +270,10 @@ __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int nteams = (gridDim.x * blockDim.x) / 32;
   const int cnt = B.counts[kCntSpill];
+  Config cfg = B.cfg;
+  cfg.flags |= OGX_F_EPA_FP64_PLANES;
   for (int j = team; j < cnt; j += nteams) {
-    epa_item<32, 0>(t, B, B.spill[j], M, false);
+    epa_item<32, 0>(t, B, cfg, B.spill[j], M, false);
     t.sync();
   }
 }

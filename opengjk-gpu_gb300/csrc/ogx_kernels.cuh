@@ -158,6 +158,30 @@ __device__ __forceinline__ void bind_src(MemBodies& s, const float* pool, BodyRe
   s.bind(pool, a, b);
 }
 
+// Store one finished pair's GJK result and route it (EPA list, FP64 refinement list).
+__device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, const GjkState& g, bool lead) {
+  const bool contact = gjk_contact(g);
+  if (lead) {
+    store_simplex(B.smp + p, g);
+    B.dist[p] = g.dist;
+    if (B.status) B.status[p] = g.status;
+    if (B.mode == kModeGjkEpa && !contact && !g.polish) store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
+    // pairs sent to the FP64 refinement get their normal there
+  }
+  const bool to_epa = lead && B.mode == kModeGjkEpa && contact;
+  const int e = warp_append(B.counts + kCntEpa + bucket, to_epa);
+  if (to_epa) B.elists[(size_t)bucket * B.npairs + e] = p;
+  const int q = warp_append(B.counts + kCntRefine, lead && g.polish);
+  if (lead && g.polish) {
+    RefineRec r;
+    r.pair = p;
+    r.wa = g.wa;
+    r.wb = g.wb;
+    r.certain = g.certain ? 1 : 0;
+    B.refine[q] = r;
+  }
+}
+
 template <int L, int K>
 __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
   const WarpTeam<L> t;
@@ -178,43 +202,65 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
     }
     GjkState g;
     gjk_pair(t, src, B.cfg, g, ws.x, ws.y);
-    const bool contact = gjk_contact(g);
-    const bool lead = t.lane() == 0;
-    if (lead) {
-      store_simplex(B.smp + p, g);
-      B.dist[p] = g.dist;
-      if (B.status) B.status[p] = g.status;
-      if (B.mode == kModeGjkEpa && !contact && !g.polish)
-        store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
-      // pairs sent to the FP64 refinement get their normal there
+    gjk_store(B, bucket, p, g, t.lane() == 0);
+  }
+}
+
+// GJK with one lane per pair and the pairs interleaved: every lane iterates its own
+// pair; a lane whose pair is done stores it and starts its next one at once, so the
+// lanes of a warp stay busy until the bucket runs out instead of waiting, pair by pair,
+// for the warp's slowest pair.  Bodies are read from memory (any size).  (L = 1 only;
+// a template so that only the translation unit listing it compiles it.)
+template <int L>
+__global__ void __launch_bounds__(128) k_gjk_il(DevBatch B, int bucket) {
+  static_assert(L == 1, "one lane per pair");
+  const WarpTeam<1> t;
+  const int nthreads = gridDim.x * blockDim.x;
+  const int cnt = B.counts[kCntGjk + bucket];
+  const int* list = B.lists + (size_t)bucket * B.npairs;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int p = 0;
+  MemBodies src;
+  GjkRun r;
+  auto begin = [&]() {
+    p = list[j];
+    const int2 pr = B.pairs[p];
+    const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
+    src.bind(B.pool, ra, rb);
+    int2 ws = make_int2(0, 0);
+    if (B.warm) {
+      ws = B.warm[p];
+      if (ws.x < 0 || ws.x >= ra.n || ws.y < 0 || ws.y >= rb.n) ws = make_int2(0, 0);
     }
-    const bool to_epa = lead && B.mode == kModeGjkEpa && contact;
-    const int e = warp_append(B.counts + kCntEpa + bucket, to_epa);
-    if (to_epa) B.elists[(size_t)bucket * B.npairs + e] = p;
-    const int q = warp_append(B.counts + kCntRefine, lead && g.polish);
-    if (lead && g.polish) {
-      RefineRec r;
-      r.pair = p;
-      r.wa = g.wa;
-      r.wb = g.wb;
-      r.certain = g.certain ? 1 : 0;
-      B.refine[q] = r;
+    gjk_start(src, r, ws.x, ws.y);
+  };
+  if (j < cnt) begin();
+  for (;;) {
+    const bool active = j < cnt;
+    if (__ballot_sync(0xffffffffu, active) == 0u) break;
+    if (active) {
+      gjk_iterate(t, src, B.cfg, r);
+      if (r.done) {
+        GjkState g;
+        gjk_end(t, src, B.cfg, r, g);
+        gjk_store(B, bucket, p, g, true);
+        j += nthreads;
+        if (j < cnt) begin();
+      }
     }
   }
 }
 
-// EPA of contact p by one team; returns false when the pair outgrew the working set
-// (small capacity only: nothing is written, the caller lists it for the full pass)
 template <int L, int K, class Mem>
-__device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, int p, Mem& M,
-                                         bool can_spill) {
+__device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
+                                         Mem& M, bool can_spill) {
   const int2 pr = B.pairs[p];
   typename SrcOf<L, K>::type src;
   bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
   GjkState g;
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
-  epa_pair(t, src, B.cfg, g, M, o, can_spill);
+  epa_pair(t, src, cfg, g, M, o, can_spill);
   if (o.spill) return false;
   const bool lead = t.lane() == 0;
   if (lead) {
@@ -244,8 +290,8 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
 }
 
 // EPA over one bucket's contacts with the small working set (EpaMemSmall per team in
-// shared memory); contacts that need more than kEpaSmallIters expansions go to the
-// spill list
+// shared memory); contacts that need more than kEpaSmallIters expansions, or whose FP32
+// expansion met an inconsistent horizon, go to the spill list
 template <int L, int K>
 __global__ void __launch_bounds__(128) k_epa(DevBatch B, int bucket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -258,7 +304,7 @@ __global__ void __launch_bounds__(128) k_epa(DevBatch B, int bucket) {
   const int* list = B.elists + (size_t)bucket * B.npairs;
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
-    const bool ok = epa_item<L, K>(t, B, p, M, B.cfg.epa_max_iter > kEpaSmallIters);
+    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true);
     const bool lead = t.lane() == 0;
     const int q = warp_append(B.counts + kCntSpill, lead && !ok);
     if (lead && !ok) B.spill[q] = p;
@@ -274,7 +320,8 @@ typedef void (*BucketKernel)(DevBatch, int);
 struct KernelInfo {
   BucketKernel fn;
   int L;  // lanes per pair
-  int K;  // float4 blocks per lane and body kept in registers (0: read from memory)
+  int K;  // float4 blocks per lane and body kept in registers (0: read from memory,
+          // -1: read from memory, pairs interleaved per lane)
 };
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant

@@ -137,6 +137,12 @@ struct Request {
   Clock::time_point t_submit, t_done;
   int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
   ogx_status err = OGX_OK;
+  // broad-phase request: the pairs come from the device grid of the version's world copy
+  bool broad = false;
+  float cell = 0.0f, margin = 0.0f;
+  int max_pairs = 0;
+  gkCollisionPair* out_pairs = nullptr;
+  int32_t* out_count = nullptr;  // [0] overlapping pairs found, [1] error flags
 };
 
 // true when p is page-locked host memory the device can copy into directly
@@ -166,7 +172,14 @@ struct Slot {
   cudaEvent_t done = nullptr;
   Request* req = nullptr;
   int world = -1;
-  bool direct[4] = {};  // results copied straight into the caller's (pinned) arrays
+  bool direct[5] = {};  // results copied straight into the caller's (pinned) arrays
+  // broad-phase requests: grid scratch, the count read back between the two stages
+  ogx_broad* broad = nullptr;
+  int* d_bres = nullptr;
+  int* h_bres = nullptr;
+  cudaEvent_t counted = nullptr;
+  int stage = 0;  // 0 idle, 1 broad phase running, 2 narrow phase running
+  int reserved = 0;  // pairs counted against the in-flight budget
 };
 
 }  // namespace
@@ -201,9 +214,14 @@ struct ogx_server {
 
   void loop();
   bool admit(Request* r, Slot& s, int w);
+  bool launch_narrow(Request* r, Slot& s, int w);
   void finish(Slot& s);
   void release();
 };
+
+ogx_status broad_run(ogx_broad* B, cudaStream_t st, const float* d_points, const ogx::BodyRef* d_bodies,
+                     int nbodies, float cell, float margin, int max_pairs, gkCollisionPair* d_pairs,
+                     int* d_result);
 
 namespace {
 
@@ -219,14 +237,48 @@ cudaError_t halloc(T** p, size_t n) {
 }  // namespace
 
 bool ogx_server::admit(Request* r, Slot& s, int w) {
-  const int n = r->npairs;
-  std::memcpy(s.h_pairs, r->pairs.data(), n * sizeof(gkCollisionPair));
   cudaStream_t st = s.ctx->stream;
   cudaError_t e = cudaStreamWaitEvent(st, world_ready[w], 0);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s.d_pairs, s.h_pairs, n * sizeof(gkCollisionPair), cudaMemcpyHostToDevice, st);
-  const int grid = std::min(grid_aux, (n + 255) / 256);
-  if (e == cudaSuccess && sc.warm_start) {
+  if (e != cudaSuccess) {
+    r->err = ogx_cuda_fail(e, "server request launch");
+    return false;
+  }
+  s.req = r;
+  s.world = w;
+  if (!r->broad) {
+    std::memcpy(s.h_pairs, r->pairs.data(), r->npairs * sizeof(gkCollisionPair));
+    e = cudaMemcpyAsync(s.d_pairs, s.h_pairs, r->npairs * sizeof(gkCollisionPair), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+      r->err = ogx_cuda_fail(e, "server request launch");
+      return false;
+    }
+    return launch_narrow(r, s, w);
+  }
+  // stage 1: pairs from the grid, count back to the host
+  const int cap = std::min(r->max_pairs, sc.slot_pairs);
+  ogx_status os = broad_run(s.broad, st, d_world[w], local->d_bodies, local->nbodies, r->cell, r->margin, cap,
+                            s.d_pairs, s.d_bres);
+  if (os) {
+    r->err = os;
+    return false;
+  }
+  e = cudaMemcpyAsync(s.h_bres, s.d_bres, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaEventRecord(s.counted, st);
+  if (e != cudaSuccess) {
+    r->err = ogx_cuda_fail(e, "server broad phase");
+    return false;
+  }
+  s.stage = 1;
+  return true;
+}
+
+bool ogx_server::launch_narrow(Request* r, Slot& s, int w) {
+  const int n = r->npairs;
+  cudaStream_t st = s.ctx->stream;
+  cudaError_t e = cudaSuccess;
+  s.stage = 2;
+  const int grid = std::max(1, std::min(grid_aux, (n + 255) / 256));
+  if (n > 0 && sc.warm_start) {
     k_warm_lookup<<<grid, 256, 0, st>>>(reinterpret_cast<const int2*>(s.d_pairs), n, d_keys, d_vals,
                                         warm_mask, s.d_warm);
     e = cudaGetLastError();
@@ -235,26 +287,28 @@ bool ogx_server::admit(Request* r, Slot& s, int w) {
     r->err = ogx_cuda_fail(e, "server request launch");
     return false;
   }
-  ogx_status os = ogx_run(s.ctx, d_world[w], local->d_bodies, local->nbodies, n, s.d_pairs, s.d_smp,
-                          s.d_dist, s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr);
+  ogx_status os = n > 0 ? ogx_run(s.ctx, d_world[w], local->d_bodies, local->nbodies, n, s.d_pairs, s.d_smp, s.d_dist,
+                                  s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr)
+                        : OGX_OK;
   if (os) {
     r->err = os;
     return false;
   }
-  if (sc.warm_start) {
+  if (n > 0 && sc.warm_start) {
     k_warm_store<<<grid, 256, 0, st>>>(reinterpret_cast<const int2*>(s.d_pairs), n, s.d_smp, d_keys, d_vals,
                                        warm_mask);
     e = cudaGetLastError();
   }
   // results go straight to the caller's arrays when those are page-locked, else through
   // the slot's pinned staging (copied out when the request completes)
-  void* dst[4] = {r->out_smp, r->out_dist, r->out_nrm, r->out_status};
-  void* stage[4] = {s.h_smp, s.h_dist, s.h_nrm, s.h_status};
-  const void* src[4] = {s.d_smp, s.d_dist, s.d_nrm, s.d_status};
-  const size_t bytes[4] = {n * sizeof(gkSimplex), n * sizeof(float), 3 * n * sizeof(float), n * sizeof(int32_t)};
-  for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+  void* dst[5] = {r->out_smp, r->out_dist, r->out_nrm, r->out_status, r->broad ? r->out_pairs : nullptr};
+  void* stage[5] = {s.h_smp, s.h_dist, s.h_nrm, s.h_status, s.h_pairs};
+  const void* src[5] = {s.d_smp, s.d_dist, s.d_nrm, s.d_status, s.d_pairs};
+  const size_t bytes[5] = {n * sizeof(gkSimplex), n * sizeof(float), 3 * n * sizeof(float), n * sizeof(int32_t),
+                           n * sizeof(gkCollisionPair)};
+  for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
     s.direct[k] = is_pinned(dst[k]);
-    if (!dst[k]) continue;
+    if (!dst[k] || n == 0) continue;
     e = cudaMemcpyAsync(s.direct[k] ? dst[k] : stage[k], src[k], bytes[k], cudaMemcpyDeviceToHost, st);
   }
   if (e == cudaSuccess) e = cudaEventRecord(s.done, st);
@@ -262,8 +316,6 @@ bool ogx_server::admit(Request* r, Slot& s, int w) {
     r->err = ogx_cuda_fail(e, "server request launch");
     return false;
   }
-  s.req = r;
-  s.world = w;
   return true;
 }
 
@@ -274,6 +326,7 @@ void ogx_server::finish(Slot& s) {
   if (r->out_dist && !s.direct[1]) std::memcpy(r->out_dist, s.h_dist, n * sizeof(float));
   if (r->out_nrm && !s.direct[2]) std::memcpy(r->out_nrm, s.h_nrm, 3 * n * sizeof(float));
   if (r->out_status && !s.direct[3]) std::memcpy(r->out_status, s.h_status, n * sizeof(int32_t));
+  if (r->broad && r->out_pairs && !s.direct[4]) std::memcpy(r->out_pairs, s.h_pairs, n * sizeof(gkCollisionPair));
 }
 
 void ogx_server::loop() {
@@ -284,28 +337,52 @@ void ogx_server::loop() {
     // completions
     for (Slot& s : slots) {
       if (!s.req) continue;
-      const cudaError_t q = cudaEventQuery(s.done);
-      if (q == cudaErrorNotReady) continue;
       Request* r = s.req;
-      if (q == cudaSuccess) {
-        finish(s);
-        r->state = 2;
+      bool failed = false;
+      if (s.stage == 1) {
+        // broad phase done: size the narrow phase by the pairs found
+        const cudaError_t q = cudaEventQuery(s.counted);
+        if (q == cudaErrorNotReady) continue;
+        if (q == cudaSuccess) {
+          const int found = s.h_bres[0];
+          if (r->out_count) {
+            r->out_count[0] = found;
+            r->out_count[1] = s.h_bres[1];
+          }
+          r->npairs = std::min(found, std::min(r->max_pairs, sc.slot_pairs));
+          failed = !launch_narrow(r, s, s.world);
+        } else {
+          r->err = ogx_cuda_fail(q, "server broad phase");
+          failed = true;
+        }
+        progress = true;
+        if (!failed) continue;
       } else {
-        r->err = ogx_cuda_fail(q, "server request");
-        r->state = 3;
+        const cudaError_t q = cudaEventQuery(s.done);
+        if (q == cudaErrorNotReady) continue;
+        if (q == cudaSuccess) {
+          finish(s);
+          r->state = 2;
+        } else {
+          r->err = ogx_cuda_fail(q, "server request");
+          failed = true;
+        }
       }
+      if (failed) r->state = 3;
       r->t_done = Clock::now();
-      pairs_in_flight -= r->npairs;
+      pairs_in_flight -= s.reserved;
       world_refs[s.world] -= 1;
       s.req = nullptr;
       s.world = -1;
+      s.stage = 0;
       progress = true;
     }
     if (progress) cv_done.notify_all();
     // admissions, oldest first
     while (!queue.empty()) {
       Request* r = queue.front();
-      if (pairs_in_flight + r->npairs > sc.max_pairs_in_flight && pairs_in_flight > 0) break;
+      const int want = r->broad ? std::min(r->max_pairs, sc.slot_pairs) : r->npairs;
+      if (pairs_in_flight + want > sc.max_pairs_in_flight && pairs_in_flight > 0) break;
       Slot* free_slot = nullptr;
       for (Slot& s : slots)
         if (!s.req) {
@@ -326,10 +403,14 @@ void ogx_server::loop() {
       if (!admit(r, *free_slot, w)) {
         r->state = 3;
         r->t_done = Clock::now();
+        free_slot->req = nullptr;
+        free_slot->world = -1;
+        free_slot->stage = 0;
         cv_done.notify_all();
         continue;
       }
-      pairs_in_flight += r->npairs;
+      free_slot->reserved = want;
+      pairs_in_flight += want;
       world_refs[w] += 1;
       progress = true;
     }
@@ -359,6 +440,10 @@ void ogx_server::release() {
     cudaFreeHost(s.h_nrm);
     cudaFreeHost(s.h_status);
     if (s.done) cudaEventDestroy(s.done);
+    if (s.broad) ogx_broad_destroy(s.broad);
+    cudaFree(s.d_bres);
+    cudaFreeHost(s.h_bres);
+    if (s.counted) cudaEventDestroy(s.counted);
   }
   slots.clear();
   for (float* p : d_world) cudaFree(p);
@@ -449,6 +534,10 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
       break;
     }
     st = s.ctx->ensure_scratch(sc.slot_pairs);
+    if (!st) st = ogx_broad_create(s.ctx, num_bodies, &s.broad);
+    if (!st && ((e = dalloc(&s.d_bres, 2)) != cudaSuccess || (e = halloc(&s.h_bres, 2)) != cudaSuccess ||
+                (e = cudaEventCreateWithFlags(&s.counted, cudaEventDisableTiming)) != cudaSuccess))
+      st = ogx_cuda_fail(e, "server broad-phase buffers");
   }
   if (!st && sc.warm_start) {
     const size_t cap = (size_t)1 << sc.warm_capacity_log2;
@@ -578,6 +667,42 @@ extern "C" ogx_status ogx_server_wait(ogx_server* S, int64_t ticket, double time
   S->reqs.erase(it);
   delete r;
   return err;
+}
+
+extern "C" ogx_status ogx_server_submit_broadphase(ogx_server* S, int64_t version, float cell, float margin,
+                                                    int max_pairs, gkCollisionPair* pairs, int32_t* count,
+                                                    gkSimplex* simplices, float* distances, float* normals,
+                                                    int32_t* status, int64_t* ticket) {
+  if (!S || !ticket) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  if (!(cell > 0.0f) || !(margin >= 0.0f) || max_pairs < 1)
+    return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
+  Request* r = new Request();
+  r->broad = true;
+  r->cell = cell;
+  r->margin = margin;
+  r->max_pairs = std::min(max_pairs, S->sc.slot_pairs);
+  r->out_pairs = pairs;
+  r->out_count = count;
+  r->out_smp = simplices;
+  r->out_dist = distances;
+  r->out_nrm = normals;
+  r->out_status = status;
+  r->version = version;
+  r->t_submit = Clock::now();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (version < 0 || version >= S->next_version ||
+        S->world_version[version % S->sc.world_slots] != version) {
+      delete r;
+      return ogx_fail(OGX_ERR_INVALID, "transform version %lld is not resident", (long long)version);
+    }
+    r->id = S->next_id++;
+    S->reqs[r->id] = r;
+    S->queue.push_back(r);
+    *ticket = r->id;
+  }
+  S->cv_work.notify_all();
+  return OGX_OK;
 }
 
 extern "C" ogx_status ogx_server_poll(ogx_server* S, int64_t ticket, int* done) {

@@ -297,6 +297,48 @@ class Graph:
             pass
 
 
+class Broad:
+    """Device broad phase (ogx_broadphase): the pairs of a pool's bodies whose boxes
+    (grown by `margin`) overlap, each once, sorted, on the device."""
+
+    def __init__(self, ctx: Context, max_bodies: int):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        check(ctx.lib.ogx_broad_create(ctx.handle, int(max_bodies), ctypes.byref(h)))
+        self.handle = h
+        self._result = _torch().zeros(2, dtype=_torch().int32, device=f"cuda:{ctx.device}")
+
+    def run(self, pool: Pool, cell: float, margin: float = 0.0, max_pairs: int = 1 << 20, pairs_dev=None):
+        """Returns (pairs int32 [n, 2] CUDA tensor, total count, error flags); waits for
+        the count."""
+        torch = _torch()
+        if pairs_dev is None:
+            pairs_dev = torch.empty((max_pairs, 2), dtype=torch.int32, device=f"cuda:{self.ctx.device}")
+        cur = torch.cuda.current_stream(pairs_dev.device)
+        if cur != self.ctx.stream:
+            self.ctx.stream.wait_stream(cur)
+        check(self.ctx.lib.ogx_broadphase(self.handle, pool.handle, float(cell), float(margin), int(max_pairs),
+                                          ctypes.c_void_p(pairs_dev.data_ptr()),
+                                          ctypes.c_void_p(self._result.data_ptr())))
+        if cur != self.ctx.stream:
+            cur.wait_stream(self.ctx.stream)
+        count, flags = (int(x) for x in self._result.cpu().tolist())
+        return pairs_dev[:min(count, max_pairs)], count, flags
+
+    def close(self):
+        if self.handle and self.ctx.handle:
+            self.ctx.lib.ogx_broad_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def query(batch, mode: int = MODE_GJK_EPA, config: _lib.Config | None = None, device: int = 0) -> dict:
     """One-shot convenience: upload a workloads.Batch, run, return host numpy results."""
     torch = _torch()

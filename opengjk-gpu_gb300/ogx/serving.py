@@ -35,6 +35,9 @@ def _bind(lib):
     lib.ogx_server_set_transforms.argtypes = [P, P, ctypes.POINTER(I64)]
     lib.ogx_server_submit.restype = ctypes.c_int
     lib.ogx_server_submit.argtypes = [P, I64, ctypes.c_int, P, P, P, P, P, ctypes.POINTER(I64)]
+    lib.ogx_server_submit_broadphase.restype = ctypes.c_int
+    lib.ogx_server_submit_broadphase.argtypes = [P, I64, ctypes.c_float, ctypes.c_float, ctypes.c_int, P, P, P, P,
+                                                 P, P, ctypes.POINTER(I64)]
     lib.ogx_server_poll.restype = ctypes.c_int
     lib.ogx_server_poll.argtypes = [P, I64, ctypes.POINTER(ctypes.c_int)]
     lib.ogx_server_wait.restype = ctypes.c_int
@@ -70,9 +73,19 @@ class Request:
         self.normal = arr(np.float32, (n, 3))
         self.status = arr(np.int32, (n,))
         self.latency_ms = None
+        self.count = None  # broad-phase requests: [pairs found, error flags]
 
     def results(self) -> dict:
-        return {"dist": self.dist, "simplex": self.simplex, "normal": self.normal, "status": self.status}
+        n = self.n_run
+        return {"dist": self.dist[:n], "simplex": self.simplex[:n], "normal": self.normal[:n],
+                "status": self.status[:n]}
+
+    @property
+    def n_run(self) -> int:
+        """Pairs the request ran (for broad-phase requests: min(found, capacity))."""
+        if self.count is None:
+            return int(self.dist.shape[0])
+        return int(min(self.count[0], self.dist.shape[0]))
 
 
 class Server:
@@ -112,6 +125,25 @@ class Server:
                                               req.normal.ctypes.data, req.status.ctypes.data, ctypes.byref(t)))
         req.ticket = t.value
         self._live[req.ticket] = req  # the arrays must outlive the request
+        return req
+
+    def submit_broadphase(self, version: int, cell: float, margin: float = 0.0, max_pairs: int = 262144) -> Request:
+        """Pairs from the device broad phase of the version's world copy (boxes grown by
+        `margin` that overlap), then GJK + EPA on them.  req.pairs[:req.n_run] are the
+        pairs run, req.count[0] the number found."""
+        t = ctypes.c_int64()
+        req = Request(0, None, max_pairs)
+        pb, pairs = _pinned(max_pairs * 8)
+        cb, cnt = _pinned(8)
+        req._bufs += [pb, cb]
+        req.pairs = pairs.view(np.int32).reshape(max_pairs, 2)
+        req.count = cnt.view(np.int32)
+        _lib.check(self.lib.ogx_server_submit_broadphase(
+            self.handle, int(version), float(cell), float(margin), int(max_pairs), req.pairs.ctypes.data,
+            req.count.ctypes.data, req.simplex.ctypes.data, req.dist.ctypes.data, req.normal.ctypes.data,
+            req.status.ctypes.data, ctypes.byref(t)))
+        req.ticket = t.value
+        self._live[req.ticket] = req
         return req
 
     def done(self, req: Request) -> bool:

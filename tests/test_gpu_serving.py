@@ -117,3 +117,27 @@ def test_admission_limits(scene):
         with pytest.raises(_lib.OgxError):
             srv.submit(v, scene.candidate_pairs(0, 10))
         assert srv.wait(srv.submit(v2, scene.candidate_pairs(2, 10))).dist.shape == (10,)
+
+
+def test_broadphase_request_matches_engine(scene, engine):
+    """A broad-phase request (device grid, then GJK + EPA, all on the device) gives the
+    standalone broad phase's pairs and the batch engine's results on them."""
+    import torch
+    xf = scene.transforms(7)
+    with _server(scene, warm_start=False) as srv:
+        v = srv.set_transforms(xf)
+        req = srv.wait(srv.submit_broadphase(v, cell=4.0, margin=0.5, max_pairs=100_000))
+    n = req.n_run
+    assert req.count[1] == 0 and n == req.count[0] > 50
+    world = scene.world(xf)
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, scene.counts)
+    pool.upload(world)
+    br = engine.Broad(ctx, scene.n_bodies)
+    pairs, count, _ = br.run(pool, 4.0, 0.5, max_pairs=100_000)
+    assert count == req.count[0]
+    assert np.array_equal(pairs.cpu().numpy(), req.pairs[:n])
+    ref = engine.run(ctx, pool, pairs.contiguous(), engine.MODE_GJK_EPA).to_host()
+    ctx.synchronize()
+    assert np.array_equal(req.dist[:n], ref["dist"])
+    assert np.array_equal(req.normal[:n], ref["normal"])

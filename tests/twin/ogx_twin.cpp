@@ -67,8 +67,12 @@ void one(const Job& J, int i, Work& M) {
     if (contact) {
       // as on the device: the small working set first, full capacity when it runs out
       EpaOut o;
-      epa_pair(t, B, *J.cfg, g, M.small, o, J.cfg->epa_max_iter > kEpaSmallIters);
-      if (o.spill) epa_pair(t, B, *J.cfg, g, M.full, o, false);
+      epa_pair(t, B, *J.cfg, g, M.small, o, true);
+      if (o.spill) {
+        ogx_config c = *J.cfg;
+        c.flags |= OGX_F_EPA_FP64_PLANES;
+        epa_pair(t, B, c, g, M.full, o, false);
+      }
       if (o.polish) epa_polish(B, o);
       d = o.dist;
       w0 = o.w0;
