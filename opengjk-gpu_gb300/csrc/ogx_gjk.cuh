@@ -526,8 +526,7 @@ OGX_HD int escalate_step(const MemBodies B, int n, const int* ia, const int* ib,
 
 // GJK as a resumable loop: gjk_start sets the state up, each gjk_iterate runs one
 // iteration (support, termination tests, sub-distance step) until r.done, gjk_end
-// finishes (witnesses, certification).  gjk_pair chains them; the interleaved kernels
-// run one iteration of a different pair in every lane.
+// finishes (witnesses, certification).  gjk_pair chains them.
 struct GjkRun {
   fv3 v;
   fv3 P[4];  // simplex in registers: slots 0..3, newest last; every index is unrolled
@@ -854,6 +853,8 @@ struct RefineState {
   Sx<double> s;
   int ia[4], ib[4];
   dv3 v;
+  double lam[4];   // barycentric weights of v on s (valid while no step changed s)
+  bool lam_valid;
   double wmax2;
   int it, max_iter;
   bool done, enclosed;
@@ -885,6 +886,11 @@ OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, Refin
         qb[q.n] = r.ib[j];
         q.n++;
       }
+    double ql[4] = {1.0, 0.0, 0.0, 0.0};
+    int m = 0;
+    for (int j = 0; j < s.n; ++j)
+      if (lam[j] > 0.0 || (s.n == 1)) ql[m++] = lam[j];
+    r.lam_valid = q.n > 0;
     if (q.n == 0) {
       q.v[0] = s.v[0];
       qa[0] = r.ia[0];
@@ -896,6 +902,7 @@ OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, Refin
       r.ia[j] = qa[j];
       r.ib[j] = qb[j];
       s.v[j].k = j;
+      r.lam[j] = ql[j];
     }
   }
   r.wmax2 = 0.0;
@@ -947,6 +954,7 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
   s.n++;
   Unc u{false};
   subdistance(s, r.v, u);
+  r.lam_valid = false;
   if (s.n != 4 && !(dot(r.v, r.v) < vv * (1.0 - 1e-12))) {
     // no progress: a tie support spanning a degenerate simplex -- keep the last answer
     s = prev;
@@ -994,11 +1002,17 @@ OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
     g.dist = 0.0f;
     return;
   }
-  dv3 P[3];
-  for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
   double lam[4];
   dv3 v;
-  closest_on_simplex(s.n, P, lam, v);
+  if (r.lam_valid) {
+    // the simplex is the one refine_begin solved: reuse its closest point
+    v = r.v;
+    for (int j = 0; j < 4; ++j) lam[j] = r.lam[j];
+  } else {
+    dv3 P[3];
+    for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
+    closest_on_simplex(s.n, P, lam, v);
+  }
   dv3 w0 = v3<double>(0.0, 0.0, 0.0), w1 = w0;
   for (int j = 0; j < s.n; ++j) {
     w0 = w0 + B.dpoint(0, r.ia[j]) * lam[j];

@@ -1,7 +1,6 @@
 // ogx_k_gjk_d.cu -- GJK bucket kernel variants that read the bodies from memory on every
 // support scan (no register copy), with 1-16 lanes per pair: many pairs per warp share
-// each instruction of the per-pair step, and the scans hit L1/L2.  K = -1: one lane per
-// pair with the pairs interleaved (k_gjk_il).
+// each instruction of the per-pair step, and the scans hit L1/L2.
 #include "ogx_kernels.cuh"
 
 namespace ogx {
@@ -9,7 +8,6 @@ namespace ogx {
 static const KernelInfo kVar[] = {
     {k_gjk<1, 0>, 1, 0}, {k_gjk<2, 0>, 2, 0}, {k_gjk<4, 0>, 4, 0},
     {k_gjk<8, 0>, 8, 0}, {k_gjk<16, 0>, 16, 0},
-    {k_gjk_il<1>, 1, -1},
 };
 
 int gjk_variants_d(const KernelInfo** out) {

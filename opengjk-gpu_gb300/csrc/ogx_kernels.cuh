@@ -206,51 +206,6 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
   }
 }
 
-// GJK with one lane per pair and the pairs interleaved: every lane iterates its own
-// pair; a lane whose pair is done stores it and starts its next one at once, so the
-// lanes of a warp stay busy until the bucket runs out instead of waiting, pair by pair,
-// for the warp's slowest pair.  Bodies are read from memory (any size).  (L = 1 only;
-// a template so that only the translation unit listing it compiles it.)
-template <int L>
-__global__ void __launch_bounds__(128) k_gjk_il(DevBatch B, int bucket) {
-  static_assert(L == 1, "one lane per pair");
-  const WarpTeam<1> t;
-  const int nthreads = gridDim.x * blockDim.x;
-  const int cnt = B.counts[kCntGjk + bucket];
-  const int* list = B.lists + (size_t)bucket * B.npairs;
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int p = 0;
-  MemBodies src;
-  GjkRun r;
-  auto begin = [&]() {
-    p = list[j];
-    const int2 pr = B.pairs[p];
-    const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
-    src.bind(B.pool, ra, rb);
-    int2 ws = make_int2(0, 0);
-    if (B.warm) {
-      ws = B.warm[p];
-      if (ws.x < 0 || ws.x >= ra.n || ws.y < 0 || ws.y >= rb.n) ws = make_int2(0, 0);
-    }
-    gjk_start(src, r, ws.x, ws.y);
-  };
-  if (j < cnt) begin();
-  for (;;) {
-    const bool active = j < cnt;
-    if (__ballot_sync(0xffffffffu, active) == 0u) break;
-    if (active) {
-      gjk_iterate(t, src, B.cfg, r);
-      if (r.done) {
-        GjkState g;
-        gjk_end(t, src, B.cfg, r, g);
-        gjk_store(B, bucket, p, g, true);
-        j += nthreads;
-        if (j < cnt) begin();
-      }
-    }
-  }
-}
-
 template <int L, int K, class Mem>
 __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
                                          Mem& M, bool can_spill) {
@@ -320,8 +275,7 @@ typedef void (*BucketKernel)(DevBatch, int);
 struct KernelInfo {
   BucketKernel fn;
   int L;  // lanes per pair
-  int K;  // float4 blocks per lane and body kept in registers (0: read from memory,
-          // -1: read from memory, pairs interleaved per lane)
+  int K;  // float4 blocks per lane and body kept in registers (0: read from memory)
 };
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
