@@ -111,8 +111,10 @@ ogx_status ogx_pool_destroy(ogx_pool* pool);
 int ogx_pool_num_bodies(const ogx_pool* pool);
 int64_t ogx_pool_num_points(const ogx_pool* pool);
 /* Load all points: xyz interleaved, bodies concatenated in index order (host memory,
- * pinned or pageable).  Asynchronous on the context's stream; pageable sources are
- * staged through the context's pinned buffer. */
+ * pinned or pageable).  Asynchronous on the context's stream.  Page-locked sources are
+ * read by the packing kernel directly over the host link (keep them unchanged until the
+ * stream passes the call, as for any asynchronous copy); pageable ones are staged
+ * through the context's pinned buffer. */
 ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* pool, const float* coords);
 /* Same from device memory (xyz interleaved, concatenated): a packing kernel. */
 ogx_status ogx_pool_load_device(ogx_ctx* ctx, ogx_pool* pool, const float* d_coords);
@@ -177,6 +179,17 @@ ogx_status ogx_broad_create(ogx_ctx* ctx, int max_bodies, ogx_broad** out);
 ogx_status ogx_broadphase(ogx_broad* broad, const ogx_pool* pool, float cell, float margin,
                           int max_pairs, gkCollisionPair* d_pairs, int* d_result);
 ogx_status ogx_broad_destroy(ogx_broad* broad);
+
+/* GJK then EPA from host memory to host memory in one call, with the transfers
+ * overlapped with the kernels: the pool's points (xyz of all bodies, concatenated, as
+ * for ogx_pool_upload) and the pairs go up in `chunks` pieces on a copy stream; each
+ * piece of the pairs runs as soon as the bodies it references are on the device; its
+ * results come back on a second copy stream while later pieces compute.  Returns when
+ * every result is in the host arrays (status may be NULL).  Page-locked host arrays
+ * let the copies run beside the kernels.  Leaves the pool loaded with xyz. */
+ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
+                                const gkCollisionPair* pairs, gkSimplex* simplices,
+                                float* distances, float* normals, int32_t* status, int chunks);
 
 /* CUDA graph of one call: captures the launches of ogx_gjk / ogx_gjk_epa / ogx_epa
  * (mode 1 / 2 / 3) on these buffers once; ogx_graph_launch replays them on the context's

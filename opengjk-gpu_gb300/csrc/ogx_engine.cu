@@ -278,6 +278,20 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
+  if (ctx->up) {
+    cudaStreamSynchronize(ctx->up);
+    cudaStreamDestroy(ctx->up);
+  }
+  if (ctx->down) {
+    cudaStreamSynchronize(ctx->down);
+    cudaStreamDestroy(ctx->down);
+  }
+  for (cudaEvent_t e : ctx->sev) cudaEventDestroy(e);
+  cudaFree(ctx->d_io_pairs);
+  cudaFree(ctx->d_io_smp);
+  cudaFree(ctx->d_io_dist);
+  cudaFree(ctx->d_io_nrm);
+  cudaFree(ctx->d_io_status);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return OGX_OK;
@@ -438,6 +452,7 @@ extern "C" ogx_status ogx_pool_create(ogx_ctx* ctx, int num_bodies, const int32_
     ogx_pool_destroy(p);
     return ogx_cuda_fail(e, "pool allocation");
   }
+  p->h_voff = voff;
   if (num_bodies > 0) {
     if ((e = cudaMemcpy(p->d_bodies, refs.data(), num_bodies * sizeof(BodyRef),
                         cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -498,6 +513,14 @@ extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* co
   const bool pinned = cudaPointerGetAttributes(&attr, coords) == cudaSuccess &&
                       (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeManaged);
   cudaGetLastError();
+  if (pinned && attr.devicePointer) {
+    // page-locked host memory is device-addressable: the packing kernel reads the
+    // caller's array directly (one pass over the host data, no staging copy)
+    ctx->last_launches = 0;
+    ogx_status s = pool_pack(ctx, p, static_cast<const float*>(attr.devicePointer));
+    if (!s) ctx->last_launches = 1;
+    return s;
+  }
   ogx_status s = ctx->ensure_stage(pinned ? 0 : bytes, bytes);
   if (s) return s;
   const void* src = coords;

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdarg.h>
 
+#include <vector>
+
 #include "ogx.h"
 #include "ogx_kernels.cuh"
 
@@ -37,6 +39,15 @@ struct ogx_ctx {
   int ev_count = 0;
 
   void mark(const char* name);  // record an event before the next launch
+  // streamed host-to-host calls: copy streams, events, device input/output buffers
+  cudaStream_t up = nullptr, down = nullptr;
+  std::vector<cudaEvent_t> sev;
+  gkCollisionPair* d_io_pairs = nullptr;
+  gkSimplex* d_io_smp = nullptr;
+  float* d_io_dist = nullptr;
+  float* d_io_nrm = nullptr;
+  int32_t* d_io_status = nullptr;
+  size_t io_cap = 0;
 
   ogx_status ensure_scratch(int npairs);
   ogx_status ensure_stage(size_t host_bytes, size_t dev_bytes);
@@ -51,6 +62,7 @@ struct ogx_pool {
   float* d_points = nullptr;
   ogx::BodyRef* d_bodies = nullptr;
   int64_t* d_voff = nullptr;  // first point of each body in the AoS source
+  std::vector<int64_t> h_voff;  // the same on the host (chunked uploads)
 };
 
 ogx_status ogx_fail(ogx_status s, const char* fmt, ...);

@@ -117,6 +117,7 @@ SIGNATURES = {
     "ogx_broad_create": (_I, [_P, _I, _P]),
     "ogx_broadphase": (_I, [_P, _P, ctypes.c_float, ctypes.c_float, _I, _P, _P]),
     "ogx_broad_destroy": (_I, [_P]),
+    "ogx_gjk_epa_streamed": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I]),
     "ogx_graph_create": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P]),
     "ogx_graph_launch": (_I, [_P]),
     "ogx_graph_kernel_launches": (_I, [_P]),

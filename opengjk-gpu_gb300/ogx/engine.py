@@ -249,6 +249,24 @@ def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Resu
     return out
 
 
+def streamed(ctx: Context, pool: Pool, coords, pairs, out: dict | None = None, chunks: int = 8) -> dict:
+    """Host-to-host GJK + EPA (ogx_gjk_epa_streamed): uploads `coords` (all bodies' xyz)
+    and `pairs` in chunks, overlapping the copies with the kernels; synchronous.
+    coords / pairs: numpy arrays or pinned torch CPU tensors; `out`: dict of host arrays
+    (simplex, dist, normal, status) to fill, allocated if None."""
+    def ptr(x):
+        return x.data_ptr() if hasattr(x, "data_ptr") else x.ctypes.data
+    n = int(pairs.shape[0])
+    if out is None:
+        out = {"simplex": np.zeros(n, SIMPLEX_DTYPE), "dist": np.zeros(n, np.float32),
+               "normal": np.zeros((n, 3), np.float32), "status": np.zeros(n, np.int32)}
+    P = ctypes.c_void_p
+    check(ctx.lib.ogx_gjk_epa_streamed(ctx.handle, pool.handle, P(ptr(coords)), n, P(ptr(pairs)),
+                                       P(ptr(out["simplex"])), P(ptr(out["dist"])), P(ptr(out["normal"])),
+                                       P(ptr(out["status"])), int(chunks)))
+    return out
+
+
 class Graph:
     """One call captured as a CUDA graph (ogx_graph_*): `launch()` replays the whole
     pipeline on the context's stream with one launch.  The pair and output buffers are

@@ -150,3 +150,41 @@ def test_graph_replay_matches_calls(engine):
     ctx.synchronize()
     assert np.array_equal(got2["dist"], ref2["dist"])
     g.close()
+
+
+def test_pinned_upload_reads_host_directly(engine):
+    """A page-locked source is packed straight from host memory; the pool equals the one
+    staged from a pageable array."""
+    import torch
+    b = W.powerlaw(seed=43, n_pairs=3000)
+    ctx = engine.Context(0)
+    pa, pb = engine.Pool(ctx, b.counts), engine.Pool(ctx, b.counts)
+    pa.upload(b.coords)
+    pinned = torch.from_numpy(b.coords).pin_memory()
+    pb.upload(pinned)
+    ctx.synchronize()
+    pairs = torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()
+    ra = engine.run(ctx, pa, pairs).to_host()
+    rb = engine.run(ctx, pb, pairs).to_host()
+    ctx.synchronize()
+    assert np.array_equal(ra["dist"], rb["dist"]) and np.array_equal(ra["normal"], rb["normal"])
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 8])
+def test_streamed_call_matches_batched(engine, chunks):
+    """The host-to-host call with overlapped chunks gives the results of the device
+    call on the same pool, for pairs that reference bodies in any order."""
+    import torch
+    b = W.powerlaw(seed=44, n_pairs=5000)
+    pairs = np.ascontiguousarray(b.pairs.copy())
+    pairs[::7] = pairs[::7][:, ::-1]            # some pairs reversed
+    pairs[100:200] = pairs[4800:4900]           # some pairs refer to late bodies early
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    coords = torch.from_numpy(b.coords).pin_memory()
+    out = engine.streamed(ctx, pool, coords, pairs, chunks=chunks)
+    ref = engine.run(ctx, pool, torch.from_numpy(pairs).cuda()).to_host()
+    ctx.synchronize()
+    assert np.array_equal(out["dist"], ref["dist"])
+    assert np.array_equal(out["normal"], ref["normal"])
+    assert np.array_equal(out["simplex"]["witnesses"], ref["simplex"]["witnesses"])
