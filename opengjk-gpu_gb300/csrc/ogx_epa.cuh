@@ -61,6 +61,8 @@ struct EpaOut {
   int face[3][2];  // vertex index pairs of the final face (FP64 re-solve)
   bool polish;
   bool spill;      // ran out of (small) capacity: nothing written, run again at full capacity
+  bool spill64;    // ... because the FP32 expansion met an inconsistent horizon: the re-run
+                   // solves every face plane in FP64
 };
 
 OGX_HD fv3 unit_or_x(fv3 d) {
@@ -294,6 +296,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   o.iters = 0;
   o.polish = false;
   o.spill = false;
+  o.spill64 = false;
   o.dist = g.dist;
   o.w0 = g.w0;
   o.w1 = g.w1;
@@ -495,6 +498,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     if (!M.vis[best]) {
       if (can_spill && escalate) {
         o.spill = true;
+        o.spill64 = true;
         return;
       }
       o.status |= OGX_S_EPA_TOPOLOGY;
@@ -529,6 +533,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     if (htot < 3) {
       if (can_spill && escalate) {
         o.spill = true;
+        o.spill64 = true;
         return;
       }
       o.status |= OGX_S_EPA_TOPOLOGY;
@@ -567,6 +572,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     if (t.any(bad)) {
       if (can_spill && escalate) {
         o.spill = true;
+        o.spill64 = true;
         return;
       }
       o.status |= OGX_S_EPA_TOPOLOGY;

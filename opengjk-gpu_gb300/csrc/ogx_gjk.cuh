@@ -1013,15 +1013,20 @@ OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
     for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
     closest_on_simplex(s.n, P, lam, v);
   }
-  dv3 w0 = v3<double>(0.0, 0.0, 0.0), w1 = w0;
+  // The distance needs the FP64 closest point; its square root and the witnesses do
+  // not: FP32 from here on (|v|^2 rounded once, then a correctly rounded sqrtf: 1 ulp;
+  // witnesses to a few ulp of the coordinates, the 1e-4 witness tolerance being far
+  // above).  FP64 issues at 1/64 of the FP32 rate here.
+  fv3 w0 = v3<float>(0.f, 0.f, 0.f), w1 = w0;
   for (int j = 0; j < s.n; ++j) {
-    w0 = w0 + B.dpoint(0, r.ia[j]) * lam[j];
-    w1 = w1 + B.dpoint(1, r.ib[j]) * lam[j];
+    const float l = (float)lam[j];
+    w0 = w0 + B.point(0, r.ia[j]) * l;
+    w1 = w1 + B.point(1, r.ib[j]) * l;
   }
   g.v = cvt<float>(v);
-  g.dist = (float)sqrt(dot(v, v));
-  g.w0 = cvt<float>(w0);
-  g.w1 = cvt<float>(w1);
+  g.dist = sqrtf((float)dot(v, v));
+  g.w0 = w0;
+  g.w1 = w1;
 }
 
 template <class Team, class Bodies>

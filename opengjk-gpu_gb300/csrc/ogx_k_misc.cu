@@ -260,8 +260,9 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// EPA at full capacity (EpaMem) over the spill list, every face plane from FP64: one warp
-// per contact, points read from memory (any body size)
+// EPA at full capacity (EpaMem) over the spill list, every face plane from FP64 for the
+// contacts whose FP32 expansion met an inconsistent horizon: one warp per contact,
+// points read from memory (any body size)
 __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMem* mem = reinterpret_cast<EpaMem*>(smem_raw);
@@ -270,10 +271,11 @@ __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int nteams = (gridDim.x * blockDim.x) / 32;
   const int cnt = B.counts[kCntSpill];
-  Config cfg = B.cfg;
-  cfg.flags |= OGX_F_EPA_FP64_PLANES;
+  Config cfg64 = B.cfg;
+  cfg64.flags |= OGX_F_EPA_FP64_PLANES;
   for (int j = team; j < cnt; j += nteams) {
-    epa_item<32, 0>(t, B, cfg, B.spill[j], M, false);
+    const int e = B.spill[j];
+    epa_item<32, 0>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
     t.sync();
   }
 }

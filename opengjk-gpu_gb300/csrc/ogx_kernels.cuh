@@ -206,9 +206,12 @@ __global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
   }
 }
 
+// spill list entries: pair index, top bit set when the re-run needs FP64 face planes
+constexpr int kSpill64 = 1 << 30;
+
 template <int L, int K, class Mem>
 __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
-                                         Mem& M, bool can_spill) {
+                                         Mem& M, bool can_spill, bool* spill64 = nullptr) {
   const int2 pr = B.pairs[p];
   typename SrcOf<L, K>::type src;
   bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
@@ -216,7 +219,10 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
   epa_pair(t, src, cfg, g, M, o, can_spill);
-  if (o.spill) return false;
+  if (o.spill) {
+    if (spill64) *spill64 = o.spill64;
+    return false;
+  }
   const bool lead = t.lane() == 0;
   if (lead) {
     B.dist[p] = o.dist;
@@ -259,10 +265,11 @@ __global__ void __launch_bounds__(128) k_epa(DevBatch B, int bucket) {
   const int* list = B.elists + (size_t)bucket * B.npairs;
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
-    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true);
+    bool s64 = false;
+    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true, &s64);
     const bool lead = t.lane() == 0;
     const int q = warp_append(B.counts + kCntSpill, lead && !ok);
-    if (lead && !ok) B.spill[q] = p;
+    if (lead && !ok) B.spill[q] = p | (s64 ? kSpill64 : 0);
     t.sync();  // the next pair reuses M
   }
 }

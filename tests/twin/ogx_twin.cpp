@@ -70,7 +70,7 @@ void one(const Job& J, int i, Work& M) {
       epa_pair(t, B, *J.cfg, g, M.small, o, true);
       if (o.spill) {
         ogx_config c = *J.cfg;
-        c.flags |= OGX_F_EPA_FP64_PLANES;
+        if (o.spill64) c.flags |= OGX_F_EPA_FP64_PLANES;
         epa_pair(t, B, c, g, M.full, o, false);
       }
       if (o.polish) epa_polish(B, o);
