@@ -106,11 +106,20 @@ int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0, g_gri
 int g_tuned[16][2][kBuckets];
 bool g_tuned_valid[16];
 
+// Persistent grid of a launch over at most `units` work items of `lanes` lanes each: the
+// full resident grid, or fewer blocks when the batch cannot fill it (small batches then
+// schedule a few blocks instead of the whole GPU for every one of the call's kernels).
+int fit_grid(int full, int units, int lanes) {
+  const long long need = ((long long)units * lanes + kBlock - 1) / kBlock;
+  return (int)std::max(1LL, std::min((long long)full, need));
+}
+
 // can variant v serve bucket b?
 bool serves(const Launch& v, int b) {
-  if (v.K <= 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
+  const int K = variant_blocks(v.K);
+  if (K == 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
   if (b == kBuckets - 1) return false;
-  const int cap = 4 * v.L * v.K;
+  const int cap = 4 * v.L * K;
   return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];
 }
 
@@ -599,13 +608,13 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     for (int b = kBuckets - 1; b >= 0; --b) {
       const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
-      k.fn<<<k.grid, kBlock, 0, st>>>(B, b);
+      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, 0, st>>>(B, b);
       ++launches;
     }
   }
   if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("refine");
-    e = launch_refine(B, g_grid_refine, g_grid_pack, st);
+    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
     launches += 3;
   }
@@ -613,18 +622,18 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     for (int b = kBuckets - 1; b >= 0; --b) {
       const Launch& k = g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
-      k.fn<<<k.grid, kBlock, k.smem, st>>>(B, b);
+      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, st>>>(B, b);
       ++launches;
     }
     // contacts that outgrew the bucket kernels' working set, at full capacity
     ctx->mark("epa_spill");
-    e = launch_epa_spill(B, g_grid_spill, st);
+    e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
     ++launches;
   }
   if (mode != kModeGjk && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("polish");
-    e = launch_polish(B, g_grid_polish, st);
+    e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
     ++launches;
   }

@@ -8,6 +8,9 @@ namespace ogx {
 static const KernelInfo kVar[] = {
     {k_gjk<1, 0>, 1, 0}, {k_gjk<2, 0>, 2, 0}, {k_gjk<4, 0>, 4, 0},
     {k_gjk<8, 0>, 8, 0}, {k_gjk<16, 0>, 16, 0},
+    // the same capped at 128 registers (4 blocks of 4 warps per SM)
+    {k_gjk<1, 0, 4>, 1, 4 << kOccShift}, {k_gjk<2, 0, 4>, 2, 4 << kOccShift},
+    {k_gjk<4, 0, 4>, 4, 4 << kOccShift}, {k_gjk<8, 0, 4>, 8, 4 << kOccShift},
 };
 
 int gjk_variants_d(const KernelInfo** out) {

@@ -182,8 +182,8 @@ __device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, 
   }
 }
 
-template <int L, int K>
-__global__ void __launch_bounds__(128) k_gjk(DevBatch B, int bucket) {
+template <int L, int K, int OCC = 1>
+__global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
   const WarpTeam<L> t;
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
@@ -282,8 +282,12 @@ typedef void (*BucketKernel)(DevBatch, int);
 struct KernelInfo {
   BucketKernel fn;
   int L;  // lanes per pair
-  int K;  // float4 blocks per lane and body kept in registers (0: read from memory)
+  int K;  // float4 blocks per lane and body kept in registers (0: read from memory);
+          // + 256 * m for a variant compiled for at least m resident blocks per SM
+          // (fewer registers per thread, more warps)
 };
+constexpr int kOccShift = 8;
+OGX_HD int variant_blocks(int K) { return K & ((1 << kOccShift) - 1); }
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
 // (L, K) can serve a bucket whose bodies have at most 4 L K points (K = 0: any size, the
