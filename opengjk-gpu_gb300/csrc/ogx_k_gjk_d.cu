@@ -11,6 +11,8 @@ static const KernelInfo kVar[] = {
     // the same capped at 128 registers (4 blocks of 4 warps per SM)
     {k_gjk<1, 0, 4>, 1, 4 << kOccShift}, {k_gjk<2, 0, 4>, 2, 4 << kOccShift},
     {k_gjk<4, 0, 4>, 4, 4 << kOccShift}, {k_gjk<8, 0, 4>, 8, 4 << kOccShift},
+    // capped at 96 registers (5 blocks per SM; a few spills)
+    {k_gjk<1, 0, 5>, 1, 5 << kOccShift}, {k_gjk<4, 0, 5>, 4, 5 << kOccShift},
 };
 
 int gjk_variants_d(const KernelInfo** out) {

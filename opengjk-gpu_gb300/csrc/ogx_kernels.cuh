@@ -253,8 +253,8 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
 // EPA over one bucket's contacts with the small working set (EpaMemSmall per team in
 // shared memory); contacts that need more than kEpaSmallIters expansions, or whose FP32
 // expansion met an inconsistent horizon, go to the spill list
-template <int L, int K>
-__global__ void __launch_bounds__(128) k_epa(DevBatch B, int bucket) {
+template <int L, int K, int OCC = 1>
+__global__ void __launch_bounds__(128, OCC) k_epa(DevBatch B, int bucket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMemSmall* mem = reinterpret_cast<EpaMemSmall*>(smem_raw);
   const WarpTeam<L> t;

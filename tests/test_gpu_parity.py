@@ -72,7 +72,7 @@ def _variant_columns(ctx):
     for kind in ("gjk", "epa"):
         for b in range(7):
             for L in (1, 2, 4, 8, 16, 32):
-                for K in (0, 1, 2, 4, 4 << 8):
+                for K in (0, 1, 2, 4, 4 << 8, 5 << 8, 1 + (5 << 8), 2 + (5 << 8)):
                     try:
                         ctx.set_kernel_choice(kind, b, L, K)
                     except _lib.OgxError:
