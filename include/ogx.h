@@ -191,6 +191,39 @@ ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, 
                                 const gkCollisionPair* pairs, gkSimplex* simplices,
                                 float* distances, float* normals, int32_t* status, int chunks);
 
+/* Collision response from the results of ogx_gjk_epa (the step after the path; the
+ * model of the reference's visualiser, visualization/integrate_final_gjk.cu:572-689):
+ * for every pair with distance <= contact_eps, a normal impulse at the witness points
+ * with the angular terms of both bodies and restitution (coefficient `restitution` when
+ * the approach speed exceeds restitution_threshold, else 0), applied only while the
+ * bodies approach, and for penetrating pairs a position correction of baumgarte * depth
+ * along the normal, shared by inverse mass.  All impulses come from the input state (a
+ * Jacobi step); each body sums its contributions in contact order, so the result is
+ * deterministic.  Body arrays are device memory: pos[n][3], quat[n][4] (x, y, z, w,
+ * body to world), vel[n][3], ang[n][3] (world frame), inv_mass[n], inv_inertia[n][3]
+ * (diagonal, body frame).  Outputs: new vel, ang, pos (device, [n][3]).  Asynchronous on
+ * the context's stream (stream-ordered scratch). */
+typedef struct ogx_body_state {
+  const float* pos;
+  const float* quat;
+  const float* vel;
+  const float* ang;
+  const float* inv_mass;
+  const float* inv_inertia;
+} ogx_body_state;
+typedef struct ogx_response_params {
+  float contact_eps;            /* default FLT_EPSILON */
+  float baumgarte;              /* default 0.2 */
+  float restitution;            /* default 0.5 */
+  float restitution_threshold;  /* default 1.0 (speed) */
+} ogx_response_params;
+void ogx_response_params_default(ogx_response_params* params);
+ogx_status ogx_contact_response(ogx_ctx* ctx, int num_bodies, const ogx_body_state* state,
+                                int npairs, const gkCollisionPair* d_pairs,
+                                const float* d_distances, const float* d_normals,
+                                const gkSimplex* d_simplices, const ogx_response_params* params,
+                                float* d_vel_out, float* d_ang_out, float* d_pos_out);
+
 /* CUDA graph of one call: captures the launches of ogx_gjk / ogx_gjk_epa / ogx_epa
  * (mode 1 / 2 / 3) on these buffers once; ogx_graph_launch replays them on the context's
  * stream with one launch.  The buffers' contents may change between launches, their

@@ -246,6 +246,18 @@ cudaError_t scan(ogx_broad* B, int* a, int n, int* total, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// exclusive scan of a[0..n) (n <= kTile * kTile) on a stream, with a caller's buffer of
+// kTile ints for the tile sums (also used by the collision response)
+ogx_status broad_scan(int* a, int n, int* total, cudaStream_t st, int* tiles) {
+  const int ntiles = (n + kTile - 1) / kTile;
+  if (ntiles > kTile) return ogx_fail(OGX_ERR_CAPACITY, "scan of %d elements", n);
+  k_tile_sums<<<ntiles, kTile, 0, st>>>(a, n, tiles);
+  k_scan_sums<<<1, kTile, 0, st>>>(tiles, ntiles, total);
+  k_tile_scan<<<ntiles, kTile, 0, st>>>(a, n, tiles);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? OGX_OK : ogx_cuda_fail(e, "scan launch");
+}
+
 extern "C" ogx_status ogx_broad_create(ogx_ctx* ctx, int max_bodies, ogx_broad** out) {
   if (!ctx || !out || max_bodies < 1) return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
   *out = nullptr;

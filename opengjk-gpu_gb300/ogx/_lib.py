@@ -63,6 +63,15 @@ class OgxError(RuntimeError):
         self.status = status
 
 
+class BodyState(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_void_p) for k in ("pos", "quat", "vel", "ang", "inv_mass", "inv_inertia")]
+
+
+class ResponseParams(ctypes.Structure):
+    _fields_ = [("contact_eps", ctypes.c_float), ("baumgarte", ctypes.c_float), ("restitution", ctypes.c_float),
+                ("restitution_threshold", ctypes.c_float)]
+
+
 class Config(ctypes.Structure):
     _fields_ = [
         ("gjk_eps_rel", ctypes.c_float),
@@ -118,6 +127,7 @@ SIGNATURES = {
     "ogx_broadphase": (_I, [_P, _P, ctypes.c_float, ctypes.c_float, _I, _P, _P]),
     "ogx_broad_destroy": (_I, [_P]),
     "ogx_gjk_epa_streamed": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I]),
+    "ogx_contact_response": (_I, [_P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "ogx_graph_create": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P]),
     "ogx_graph_launch": (_I, [_P]),
     "ogx_graph_kernel_launches": (_I, [_P]),

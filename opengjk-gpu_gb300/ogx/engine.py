@@ -267,6 +267,30 @@ def streamed(ctx: Context, pool: Pool, coords, pairs, out: dict | None = None, c
     return out
 
 
+def contact_response(ctx: Context, state: dict, pairs_dev, res: Results, baumgarte: float = 0.2,
+                     restitution: float = 0.5, restitution_threshold: float = 1.0,
+                     contact_eps: float = 1.1920929e-07) -> dict:
+    """Collision response (ogx_contact_response) from a GJK+EPA result: `state` holds
+    CUDA float32 tensors pos [n,3], quat [n,4] (x,y,z,w), vel [n,3], ang [n,3],
+    inv_mass [n], inv_inertia [n,3]; returns new vel, ang, pos tensors."""
+    torch = _torch()
+    n = int(state["pos"].shape[0])
+    st = _lib.BodyState(*(state[k].data_ptr() for k in ("pos", "quat", "vel", "ang", "inv_mass", "inv_inertia")))
+    prm = _lib.ResponseParams(contact_eps, baumgarte, restitution, restitution_threshold)
+    out = {k: torch.empty((n, 3), dtype=torch.float32, device=state["pos"].device) for k in ("vel", "ang", "pos")}
+    cur = torch.cuda.current_stream(pairs_dev.device)
+    if cur != ctx.stream:
+        ctx.stream.wait_stream(cur)
+    P = ctypes.c_void_p
+    check(ctx.lib.ogx_contact_response(ctx.handle, n, ctypes.byref(st), int(pairs_dev.shape[0]),
+                                       P(pairs_dev.data_ptr()), P(res.dist.data_ptr()), P(res.normal.data_ptr()),
+                                       P(res.simplex.data_ptr()), ctypes.byref(prm), P(out["vel"].data_ptr()),
+                                       P(out["ang"].data_ptr()), P(out["pos"].data_ptr())))
+    if cur != ctx.stream:
+        cur.wait_stream(ctx.stream)
+    return out
+
+
 class Graph:
     """One call captured as a CUDA graph (ogx_graph_*): `launch()` replays the whole
     pipeline on the context's stream with one launch.  The pair and output buffers are
