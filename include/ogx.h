@@ -191,6 +191,24 @@ ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, 
                                 const gkCollisionPair* pairs, gkSimplex* simplices,
                                 float* distances, float* normals, int32_t* status, int chunks);
 
+/* Bodies made of several convex parts (a convex decomposition; parts are the pool's
+ * bodies, body B owns parts [first[B], first[B] + count[B])).  Expansion of body pairs
+ * into part pairs, as the reference's visualiser does it
+ * (visualization/integrate_final_gjk.cu:265-302): body pair p becomes
+ * (first[A] + a, first[B] + b) for every a, b, a-major, body pairs in order.
+ * d_offsets[num_body_pairs + 1] receives each body pair's first part pair (last entry:
+ * the total; only the first max_sub_pairs are written); d_owner (optional) the body pair
+ * of each part pair.  The reduction gives per body pair the smallest part-pair distance
+ * (closest or most penetrating) and its part-pair index.  Device arrays, asynchronous. */
+ogx_status ogx_expand_submesh_pairs(ogx_ctx* ctx, int num_body_pairs,
+                                    const gkCollisionPair* d_body_pairs, int num_bodies,
+                                    const int32_t* d_first_part, const int32_t* d_part_count,
+                                    int max_sub_pairs, gkCollisionPair* d_sub_pairs,
+                                    int32_t* d_owner, int32_t* d_offsets);
+ogx_status ogx_reduce_submesh_pairs(ogx_ctx* ctx, int num_body_pairs, const int32_t* d_offsets,
+                                    int max_sub_pairs, const float* d_sub_distances,
+                                    float* d_best_distance, int32_t* d_best_index);
+
 /* Collision response from the results of ogx_gjk_epa (the step after the path; the
  * model of the reference's visualiser, visualization/integrate_final_gjk.cu:572-689):
  * for every pair with distance <= contact_eps, a normal impulse at the witness points

@@ -219,6 +219,52 @@ __global__ void k_pairs(const float4* __restrict__ lo, const float4* __restrict_
 
 }  // namespace
 
+// ---------------------------------------------------------------------------------
+// bodies made of several convex parts (sub-meshes): pair expansion and reduction
+
+static __global__ void k_sub_count(const int2* __restrict__ bp, int n, const int* __restrict__ cnt, int nb,
+                            int* __restrict__ out) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int2 q = bp[p];
+    const bool ok = q.x >= 0 && q.x < nb && q.y >= 0 && q.y < nb;
+    out[p] = ok ? cnt[q.x] * cnt[q.y] : 0;
+  }
+}
+
+static __global__ void k_sub_expand(const int2* __restrict__ bp, int n, const int* __restrict__ first,
+                             const int* __restrict__ cnt, int nb, const int* __restrict__ off, int cap,
+                             int2* __restrict__ sub, int* __restrict__ owner) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int2 q = bp[p];
+    if (!(q.x >= 0 && q.x < nb && q.y >= 0 && q.y < nb)) continue;
+    const int fa = first[q.x], ca = cnt[q.x], fb = first[q.y], cb = cnt[q.y];
+    int w = off[p];
+    for (int a = 0; a < ca; ++a)
+      for (int b = 0; b < cb; ++b, ++w)
+        if (w < cap) {
+          sub[w] = make_int2(fa + a, fb + b);
+          if (owner) owner[w] = p;
+        }
+  }
+}
+
+// smallest distance (most penetrating) over each body pair's parts; -1 / +inf when none
+static __global__ void k_sub_reduce(const int* __restrict__ off, int n, int cap, const float* __restrict__ dist,
+                             float* __restrict__ best, int* __restrict__ arg) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int e = min(off[p + 1], cap);
+    float b = INFINITY;
+    int k = -1;
+    for (int i = off[p]; i < e; ++i)
+      if (dist[i] < b) {
+        b = dist[i];
+        k = i;
+      }
+    best[p] = b;
+    if (arg) arg[p] = k;
+  }
+}
+
 struct ogx_broad {
   ogx_ctx* ctx = nullptr;
   int max_bodies = 0;
@@ -359,4 +405,55 @@ extern "C" ogx_status ogx_broadphase(ogx_broad* B, const ogx_pool* pool, float c
   cudaSetDevice(B->ctx->device);
   return broad_run(B, B->ctx->stream, pool->d_points, pool->d_bodies, pool->nbodies, cell, margin, max_pairs,
                    d_pairs, d_result);
+}
+
+// Sub-mesh pair expansion (visualization/integrate_final_gjk.cu:265-302): body pair p of
+// bodies A, B becomes parts (first[A] + a, first[B] + b) for a < count[A], b < count[B],
+// a-major, body pairs in order.  d_offsets[num_body_pairs + 1] receives each body pair's
+// first expanded pair (the last entry = the total, which may exceed max_sub_pairs: then
+// only the first max_sub_pairs are written).  d_owner (optional) gets the body pair of
+// each expanded pair.
+extern "C" ogx_status ogx_expand_submesh_pairs(ogx_ctx* ctx, int num_body_pairs, const gkCollisionPair* d_body_pairs,
+                                               int num_bodies, const int32_t* d_first_part,
+                                               const int32_t* d_part_count, int max_sub_pairs,
+                                               gkCollisionPair* d_sub_pairs, int32_t* d_owner, int32_t* d_offsets) {
+  if (!ctx || num_body_pairs < 0 || num_bodies < 0 || max_sub_pairs < 0 || !d_offsets ||
+      (num_body_pairs > 0 && (!d_body_pairs || !d_first_part || !d_part_count || !d_sub_pairs)))
+    return ogx_fail(OGX_ERR_INVALID, "bad expansion arguments");
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  int* tiles = nullptr;
+  cudaError_t e = cudaMallocAsync(&tiles, kTile * sizeof(int), st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "expansion scratch");
+  const int g = std::max(1, std::min(8 * ctx->sm_count, (num_body_pairs + 255) / 256));
+  e = cudaMemsetAsync(d_offsets + num_body_pairs, 0, sizeof(int), st);
+  if (e == cudaSuccess && num_body_pairs > 0)
+    k_sub_count<<<g, 256, 0, st>>>(reinterpret_cast<const int2*>(d_body_pairs), num_body_pairs, d_part_count,
+                                   num_bodies, d_offsets);
+  ogx_status s = e == cudaSuccess ? broad_scan(d_offsets, num_body_pairs + 1, nullptr, st, tiles)
+                                  : ogx_cuda_fail(e, "expansion");
+  if (!s && num_body_pairs > 0) {
+    k_sub_expand<<<g, 256, 0, st>>>(reinterpret_cast<const int2*>(d_body_pairs), num_body_pairs, d_first_part,
+                                    d_part_count, num_bodies, d_offsets, max_sub_pairs,
+                                    reinterpret_cast<int2*>(d_sub_pairs), d_owner);
+    if ((e = cudaGetLastError()) != cudaSuccess) s = ogx_cuda_fail(e, "expansion launch");
+  }
+  cudaFreeAsync(tiles, st);
+  return s;
+}
+
+// Per body pair, the smallest distance over its expanded pairs (the closest or most
+// penetrating part pair) and its index (-1 and +inf for a body pair with no parts).
+extern "C" ogx_status ogx_reduce_submesh_pairs(ogx_ctx* ctx, int num_body_pairs, const int32_t* d_offsets,
+                                               int max_sub_pairs, const float* d_sub_distances,
+                                               float* d_best_distance, int32_t* d_best_index) {
+  if (!ctx || num_body_pairs < 0 || (num_body_pairs > 0 && (!d_offsets || !d_sub_distances || !d_best_distance)))
+    return ogx_fail(OGX_ERR_INVALID, "bad reduction arguments");
+  if (num_body_pairs == 0) return OGX_OK;
+  cudaSetDevice(ctx->device);
+  const int g = std::max(1, std::min(8 * ctx->sm_count, (num_body_pairs + 255) / 256));
+  k_sub_reduce<<<g, 256, 0, ctx->stream>>>(d_offsets, num_body_pairs, max_sub_pairs, d_sub_distances,
+                                           d_best_distance, d_best_index);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? OGX_OK : ogx_cuda_fail(e, "reduction launch");
 }

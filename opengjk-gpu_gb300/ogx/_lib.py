@@ -128,6 +128,8 @@ SIGNATURES = {
     "ogx_broad_destroy": (_I, [_P]),
     "ogx_gjk_epa_streamed": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I]),
     "ogx_contact_response": (_I, [_P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "ogx_expand_submesh_pairs": (_I, [_P, _I, _P, _I, _P, _P, _I, _P, _P, _P]),
+    "ogx_reduce_submesh_pairs": (_I, [_P, _I, _P, _I, _P, _P, _P]),
     "ogx_graph_create": (_I, [_P, _P, _I, _P, _P, _P, _P, _P, _I, _P]),
     "ogx_graph_launch": (_I, [_P]),
     "ogx_graph_kernel_launches": (_I, [_P]),

@@ -291,6 +291,47 @@ def contact_response(ctx: Context, state: dict, pairs_dev, res: Results, baumgar
     return out
 
 
+def expand_submesh_pairs(ctx: Context, body_pairs_dev, first_part_dev, part_count_dev, max_sub_pairs: int):
+    """Body pairs -> part pairs (ogx_expand_submesh_pairs): returns (part pairs [m, 2],
+    owner body pair [m], offsets [n + 1]) as CUDA tensors; waits for the total."""
+    torch = _torch()
+    n = int(body_pairs_dev.shape[0])
+    dev = body_pairs_dev.device
+    sub = torch.empty((max(max_sub_pairs, 1), 2), dtype=torch.int32, device=dev)
+    owner = torch.empty(max(max_sub_pairs, 1), dtype=torch.int32, device=dev)
+    off = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    cur = torch.cuda.current_stream(dev)
+    if cur != ctx.stream:
+        ctx.stream.wait_stream(cur)
+    P = ctypes.c_void_p
+    check(ctx.lib.ogx_expand_submesh_pairs(ctx.handle, n, P(body_pairs_dev.data_ptr()), int(first_part_dev.shape[0]),
+                                           P(first_part_dev.data_ptr()), P(part_count_dev.data_ptr()),
+                                           int(max_sub_pairs), P(sub.data_ptr()), P(owner.data_ptr()),
+                                           P(off.data_ptr())))
+    if cur != ctx.stream:
+        cur.wait_stream(ctx.stream)
+    total = int(off[n].item())
+    m = min(total, max_sub_pairs)
+    return sub[:m], owner[:m], off
+
+
+def reduce_submesh_pairs(ctx: Context, offsets_dev, sub_dist_dev, max_sub_pairs: int):
+    """Per body pair: (smallest part-pair distance, its part-pair index) CUDA tensors."""
+    torch = _torch()
+    n = int(offsets_dev.shape[0]) - 1
+    best = torch.empty(max(n, 1), dtype=torch.float32, device=offsets_dev.device)
+    arg = torch.empty(max(n, 1), dtype=torch.int32, device=offsets_dev.device)
+    cur = torch.cuda.current_stream(offsets_dev.device)
+    if cur != ctx.stream:
+        ctx.stream.wait_stream(cur)
+    P = ctypes.c_void_p
+    check(ctx.lib.ogx_reduce_submesh_pairs(ctx.handle, n, P(offsets_dev.data_ptr()), int(max_sub_pairs),
+                                           P(sub_dist_dev.data_ptr()), P(best.data_ptr()), P(arg.data_ptr())))
+    if cur != ctx.stream:
+        cur.wait_stream(ctx.stream)
+    return best[:n], arg[:n]
+
+
 class Graph:
     """One call captured as a CUDA graph (ogx_graph_*): `launch()` replays the whole
     pipeline on the context's stream with one launch.  The pair and output buffers are

@@ -118,8 +118,15 @@ def test_response_pushes_bodies_apart(engine):
              "inv_inertia": f([[1, 1, 1], [1, 1, 1]])}
     out = engine.contact_response(ctx, state, pairs, res, restitution=0.0)
     ctx.synchronize()
-    v = out["vel"].cpu().numpy()
+    v = out["vel"].cpu().numpy().astype(np.float64)
+    w = out["ang"].cpu().numpy().astype(np.float64)
     p = out["pos"].cpu().numpy()
-    assert res.dist.cpu().numpy()[0] < 0
-    assert v[1, 0] - v[0, 0] >= -1e-5          # no longer approaching along x
-    assert p[0, 0] < 0 < p[1, 0] - 1.5         # positions corrected apart
+    h = res.to_host()
+    n = h["normal"][0].astype(np.float64)
+    wit = h["simplex"]["witnesses"][0].astype(np.float64)
+    assert h["dist"][0] < 0 and n[0] > 0.99      # normal from body 1 towards body 2
+    ra, rb = wit[0] - [0, 0, 0], wit[1] - [1.5, 0, 0]
+    vn = ((v[1] + np.cross(w[1], rb)) - (v[0] + np.cross(w[0], ra))) @ n
+    assert vn >= -1e-5                            # no longer approaching at the contact
+    assert v[0, 0] < 2 and v[1, 0] > -2          # both slowed along the normal
+    assert p[0, 0] < 0 < p[1, 0] - 1.5           # positions corrected apart
