@@ -296,6 +296,14 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
     cudaStreamDestroy(ctx->down);
   }
   for (cudaEvent_t e : ctx->sev) cudaEventDestroy(e);
+  for (int b = 0; b < kBuckets; ++b) {
+    if (ctx->aux[b]) {
+      cudaStreamSynchronize(ctx->aux[b]);
+      cudaStreamDestroy(ctx->aux[b]);
+    }
+    if (ctx->join_ev[b]) cudaEventDestroy(ctx->join_ev[b]);
+  }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   cudaFree(ctx->d_io_pairs);
   cudaFree(ctx->d_io_smp);
   cudaFree(ctx->d_io_dist);
@@ -399,6 +407,19 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
     return ogx_cuda_fail(e, "scratch allocation");
   }
   cap_pairs = cap;
+  return OGX_OK;
+}
+
+ogx_status ogx_ctx::ensure_aux() {
+  if (fork_ev) return OGX_OK;
+  cudaError_t e;
+  for (int b = 0; b < kBuckets; ++b) {
+    if ((e = cudaStreamCreateWithFlags(&aux[b], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&join_ev[b], cudaEventDisableTiming)) != cudaSuccess)
+      return ogx_cuda_fail(e, "bucket streams");
+  }
+  if ((e = cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming)) != cudaSuccess)
+    return ogx_cuda_fail(e, "bucket streams");
   return OGX_OK;
 }
 
@@ -604,13 +625,36 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   e = launch_bin(B, bin_grid, st);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "k_bin launch");
   ++launches;
+  // The seven bucket kernels of a stage run concurrently (one stream each, forked from
+  // and joined back into the context's stream) so that the tail of one bucket overlaps
+  // the others' work; with per-kernel timing on they run in sequence.
+  const bool fork = !ctx->timing && ctx->ensure_aux() == OGX_OK;
+  auto bucket_stream = [&](int b) -> cudaStream_t { return fork ? ctx->aux[b] : st; };
+  auto fork_out = [&]() -> cudaError_t {
+    if (!fork) return cudaSuccess;
+    cudaError_t r = cudaEventRecord(ctx->fork_ev, st);
+    for (int b = 0; b < kBuckets && r == cudaSuccess; ++b) r = cudaStreamWaitEvent(ctx->aux[b], ctx->fork_ev, 0);
+    return r;
+  };
+  auto join_in = [&]() -> cudaError_t {
+    if (!fork) return cudaSuccess;
+    cudaError_t r = cudaSuccess;
+    for (int b = 0; b < kBuckets && r == cudaSuccess; ++b) {
+      r = cudaEventRecord(ctx->join_ev[b], ctx->aux[b]);
+      if (r == cudaSuccess) r = cudaStreamWaitEvent(st, ctx->join_ev[b], 0);
+    }
+    return r;
+  };
   if (mode != kModeEpa) {
-    for (int b = kBuckets - 1; b >= 0; --b) {
+    e = fork_out();
+    for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
       const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
-      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, 0, st>>>(B, b);
+      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, 0, bucket_stream(b)>>>(B, b);
       ++launches;
     }
+    if (e == cudaSuccess) e = join_in();
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "GJK launches");
   }
   if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("refine");
@@ -619,12 +663,15 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     launches += 3;
   }
   if (mode != kModeGjk) {
-    for (int b = kBuckets - 1; b >= 0; --b) {
+    e = fork_out();
+    for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
       const Launch& k = g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
-      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, st>>>(B, b);
+      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
       ++launches;
     }
+    if (e == cudaSuccess) e = join_in();
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA launches");
     // contacts that outgrew the bucket kernels' working set, at full capacity
     ctx->mark("epa_spill");
     e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), st);

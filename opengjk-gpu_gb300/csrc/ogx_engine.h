@@ -39,6 +39,11 @@ struct ogx_ctx {
   int ev_count = 0;
 
   void mark(const char* name);  // record an event before the next launch
+  // concurrent bucket launches: one stream per size bucket, fork / join events
+  cudaStream_t aux[ogx::kBuckets] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[ogx::kBuckets] = {};
+  ogx_status ensure_aux();
   // streamed host-to-host calls: copy streams, events, device input/output buffers
   cudaStream_t up = nullptr, down = nullptr;
   std::vector<cudaEvent_t> sev;
