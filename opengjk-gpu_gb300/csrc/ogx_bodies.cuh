@@ -14,28 +14,10 @@
 
 namespace ogx {
 
-// Bounded support scans for large bodies.  A body above kAccMin points gets, when the
-// pool is loaded, its points grouped into kAccBins bins by the direction from the body's
-// centroid (octant x dominant axis) with each bin's axis-aligned box; the support scan
-// then bounds every bin by its box, evaluates the bin with the highest bound, and only
-// the bins whose bound (plus the rounding margin of the FP32 dot products) reaches the
-// best value found.  The result -- the first maximum of fl(p . d) in point order -- is
-// the full scan's, bit for bit.
-constexpr int kAccBins = 24;
-constexpr int kAccMin = 129;      // bodies of at least this many points get bins
-constexpr int kAccMax = 65535;    // ... and at most this many (16-bit point lists)
-struct AccRef {
-  int bins;  // first bin record of the body (2 float4 per bin), < 0: no bins
-  int idx;   // first entry of the body's point list (point indices grouped by bin)
-};
-
 struct MemBodies {
   const float* base[2];  // x[0] of each body
   int n[2];
   int n4[2];
-  const float4* acc_bins;  // null: full scans
-  const uint16_t* acc_idx;
-  AccRef acc[2];
 
   OGX_HD void bind(const float* pool, BodyRef a, BodyRef b) {
     base[0] = pool + 4 * (size_t)a.quad;
@@ -44,16 +26,6 @@ struct MemBodies {
     n[1] = b.n;
     n4[0] = round4(a.n);
     n4[1] = round4(b.n);
-    acc_bins = nullptr;
-    acc_idx = nullptr;
-    acc[0].bins = acc[1].bins = -1;
-    acc[0].idx = acc[1].idx = 0;
-  }
-  OGX_HD void bind_acc(const float4* bins, const uint16_t* idx, AccRef a, AccRef b) {
-    acc_bins = bins;
-    acc_idx = idx;
-    acc[0] = a;
-    acc[1] = b;
   }
   OGX_HD fv3 point(int w, int i) const {
     const float* p = base[w];
@@ -85,82 +57,8 @@ struct MemBodies {
     }
   }
 
-  // lane-local best over the candidate bins of body w (see kAccBins); the team argmax of
-  // the lanes' results is the full scan's
-  template <class Team>
-  OGX_HD void scan_bins(const Team& t, int w, fv3 d, float& best, int& bi) const {
-    const float4* bins = acc_bins + 2 * acc[w].bins;
-    const uint16_t* I = acc_idx + acc[w].idx;
-    const float* X = base[w];
-    const float* Y = X + n4[w];
-    const float* Z = X + 2 * n4[w];
-    const int L = Team::L;
-    const int lane = t.lane();
-    // bounds: lane l takes bins l, l + L, ...; a candidate mask over all bins for the team
-    float ub_best = -INFINITY;
-    int b_best = -1;
-    uint32_t mask = 0u;
-    constexpr int R = (kAccBins + Team::L - 1) / Team::L;
-    float my_ub[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int b = r * L + lane;
-      float ub = -INFINITY;
-      if (b < kAccBins) {
-        const float4 lo = bins[2 * b], hi = bins[2 * b + 1];
-        const int cnt = f32_bits(hi.w);
-        if (cnt > 0) {
-          const float sx = d.x >= 0.0f ? d.x * hi.x : d.x * lo.x;
-          const float sy = d.y >= 0.0f ? d.y * hi.y : d.y * lo.y;
-          const float sz = d.z >= 0.0f ? d.z * hi.z : d.z * lo.z;
-          const float mag = fabsf(d.x) * fmaxf(fabsf(lo.x), fabsf(hi.x)) +
-                            fabsf(d.y) * fmaxf(fabsf(lo.y), fabsf(hi.y)) +
-                            fabsf(d.z) * fmaxf(fabsf(lo.z), fabsf(hi.z));
-          ub = (sx + sy + sz) + 8.0f * FLT_EPSILON * mag;
-        }
-      }
-      my_ub[r] = ub;
-      if (ub > ub_best) {
-        ub_best = ub;
-        b_best = b;
-      }
-    }
-    // the bin with the highest bound first
-    t.argmax(ub_best, b_best);
-    best = -INFINITY;
-    bi = 0x7fffffff;
-    auto eval_bin = [&](int b) {
-      const float4 lo = bins[2 * b], hi = bins[2 * b + 1];
-      const int start = f32_bits(lo.w), cnt = f32_bits(hi.w);
-      for (int j = lane; j < cnt; j += L) {
-        const int i = I[start + j];
-        const float v = sdot(X[i], Y[i], Z[i], d);
-        if (v > best || (v == best && i < bi)) {
-          best = v;
-          bi = i;
-        }
-      }
-    };
-    if (b_best >= 0) eval_bin(b_best);
-    float tb = best;
-    int ti = bi;
-    t.argmax(tb, ti);
-    // every other bin whose bound reaches the best value so far
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const int b = r * L + lane;
-      const bool c = b < kAccBins && b != b_best && my_ub[r] >= tb;
-      mask |= t.ballot(c) << (r * L);
-    }
-    for (uint32_t m = mask; m != 0u; m &= m - 1u) eval_bin(ctz32(m));
-  }
-
   template <class Team>
   OGX_HD void scan(const Team& t, int w, fv3 d, float& best, int& bi) const {
-    if (acc_bins && acc[w].bins >= 0) {
-      scan_bins(t, w, d, best, bi);
-      return;
-    }
     best = -INFINITY;
     bi = 0x7fffffff;
     const int nb = n4[w] >> 2;

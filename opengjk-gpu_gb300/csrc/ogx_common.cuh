@@ -12,8 +12,6 @@
 // fmaf() explicitly, so the host build and the device build round identically.
 #pragma once
 
-#include <string.h>
-
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
@@ -178,34 +176,6 @@ OGX_HD Config reference_config() {
   c.flags = OGX_F_REFERENCE_TOL;
   c.polish_rel = 0.0f;
   return c;
-}
-
-OGX_HD int ctz32(uint32_t x) {
-#if defined(__CUDA_ARCH__)
-  return __ffs((int)x) - 1;
-#else
-  return __builtin_ctz(x);
-#endif
-}
-
-OGX_HD int f32_bits(float x) {
-#if defined(__CUDA_ARCH__)
-  return __float_as_int(x);
-#else
-  int i;
-  memcpy(&i, &x, sizeof(i));
-  return i;
-#endif
-}
-
-OGX_HD float bits_f32(int i) {
-#if defined(__CUDA_ARCH__)
-  return __int_as_float(i);
-#else
-  float x;
-  memcpy(&x, &i, sizeof(x));
-  return x;
-#endif
 }
 
 OGX_HD int popc32(uint32_t x) {

@@ -117,7 +117,7 @@ int fit_grid(int full, int units, int lanes) {
 // can variant v serve bucket b?
 bool serves(const Launch& v, int b) {
   const int K = variant_blocks(v.K);
-  if (K == 0) return true;  // memory scans (bounded by the bins for large bodies): any size
+  if (K == 0) return v.L == 32 || b < kBuckets - 1 || v.L >= 8;  // memory-streamed: any size
   if (b == kBuckets - 1) return false;
   const int cap = 4 * v.L * K;
   return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];
@@ -483,30 +483,6 @@ extern "C" ogx_status ogx_pool_create(ogx_ctx* ctx, int num_bodies, const int32_
     return ogx_cuda_fail(e, "pool allocation");
   }
   p->h_voff = voff;
-  // bins for the large bodies
-  std::vector<AccRef> acc(num_bodies);
-  int64_t acc_pts = 0;
-  int nacc = 0;
-  for (int b = 0; b < num_bodies; ++b) {
-    if (counts[b] >= kAccMin && counts[b] <= kAccMax && acc_pts + counts[b] < (1ll << 31)) {
-      acc[b].bins = nacc * kAccBins;
-      acc[b].idx = (int)acc_pts;
-      acc_pts += counts[b];
-      ++nacc;
-    } else {
-      acc[b].bins = -1;
-      acc[b].idx = 0;
-    }
-  }
-  p->nacc = nacc;
-  if (nacc > 0 &&
-      ((e = cudaMalloc(&p->d_acc, num_bodies * sizeof(AccRef))) != cudaSuccess ||
-       (e = cudaMalloc(&p->d_acc_bins, (size_t)nacc * kAccBins * 2 * sizeof(float4))) != cudaSuccess ||
-       (e = cudaMalloc(&p->d_acc_idx, std::max<int64_t>(8, acc_pts) * sizeof(uint16_t))) != cudaSuccess ||
-       (e = cudaMemcpy(p->d_acc, acc.data(), num_bodies * sizeof(AccRef), cudaMemcpyHostToDevice)) != cudaSuccess)) {
-    ogx_pool_destroy(p);
-    return ogx_cuda_fail(e, "pool bin allocation");
-  }
   if (num_bodies > 0) {
     if ((e = cudaMemcpy(p->d_bodies, refs.data(), num_bodies * sizeof(BodyRef),
                         cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -527,9 +503,6 @@ extern "C" ogx_status ogx_pool_destroy(ogx_pool* p) {
   cudaFree(p->d_points);
   cudaFree(p->d_bodies);
   cudaFree(p->d_voff);
-  cudaFree(p->d_acc);
-  cudaFree(p->d_acc_bins);
-  cudaFree(p->d_acc_idx);
   delete p;
   return OGX_OK;
 }
@@ -544,20 +517,12 @@ extern "C" ogx_status ogx_pool_device_layout(const ogx_pool* p, float** d_points
   return OGX_OK;
 }
 
-// pack bodies [b0, b1) from AoS into the pool layout and build their bins
-ogx_status pool_pack_range(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos, int b0, int b1, cudaStream_t st) {
-  const int n = b1 - b0;
-  if (n <= 0) return OGX_OK;
-  const int grid = std::max(1, std::min(g_grid_pack, (n + 7) / 8));
-  cudaError_t e = launch_pack(d_aos, p->d_voff + b0, p->d_bodies + b0, n, p->d_points, grid, st);
-  if (e == cudaSuccess && p->nacc > 0)
-    e = launch_accel(p->d_points, p->d_bodies + b0, p->d_acc + b0, n, p->d_acc_bins, p->d_acc_idx, grid, st);
+ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos) {
+  if (p->nbodies == 0) return OGX_OK;
+  cudaError_t e = launch_pack(d_aos, p->d_voff, p->d_bodies, p->nbodies, p->d_points, g_grid_pack,
+                              ctx->stream);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "k_pack launch");
   return OGX_OK;
-}
-
-ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos) {
-  return pool_pack_range(ctx, p, d_aos, 0, p->nbodies, ctx->stream);
 }
 
 extern "C" ogx_status ogx_pool_load_device(ogx_ctx* ctx, ogx_pool* p, const float* d_coords) {
@@ -615,7 +580,7 @@ extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* co
 
 ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, int nbodies,
                    int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
-                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm, PoolAcc acc) {
+                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm) {
   if (npairs < 0) return ogx_fail(OGX_ERR_INVALID, "npairs < 0");
   if (npairs == 0) {
     ctx->last_launches = 0;
@@ -644,9 +609,6 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.refine_full = ctx->d_refine_full;
   B.spill = ctx->d_spill;
   B.warm = d_warm;
-  B.acc_refs = acc.refs;
-  B.acc_bins = acc.bins;
-  B.acc_idx = acc.idx;
   B.cfg = ctx->cfg;
   B.mode = mode;
   cudaStream_t st = ctx->stream;
@@ -734,7 +696,7 @@ extern "C" ogx_status ogx_gjk(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                               float* d_distances, int32_t* d_status) {
   if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
   return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
-                 d_distances, nullptr, d_status, kModeGjk, nullptr, pool->acc());
+                 d_distances, nullptr, d_status, kModeGjk);
 }
 
 extern "C" ogx_status ogx_gjk_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
@@ -742,7 +704,7 @@ extern "C" ogx_status ogx_gjk_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs
                                   float* d_distances, float* d_normals, int32_t* d_status) {
   if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
   return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
-                 d_distances, d_normals, d_status, kModeGjkEpa, nullptr, pool->acc());
+                 d_distances, d_normals, d_status, kModeGjkEpa);
 }
 
 extern "C" ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
@@ -750,7 +712,7 @@ extern "C" ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                               float* d_distances, float* d_normals, int32_t* d_status) {
   if (!ctx || !pool) return ogx_fail(OGX_ERR_INVALID, "NULL context or pool");
   return ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices,
-                 d_distances, d_normals, d_status, kModeEpa, nullptr, pool->acc());
+                 d_distances, d_normals, d_status, kModeEpa);
 }
 
 // ---------------------------------------------------------------------------------
@@ -809,7 +771,7 @@ extern "C" ogx_status ogx_graph_create(ogx_ctx* ctx, const ogx_pool* pool, int n
     return ogx_cuda_fail(e, "cudaStreamBeginCapture");
   }
   s = ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, d_simplices, d_distances,
-              d_normals, d_status, mode, nullptr, pool->acc());
+              d_normals, d_status, mode);
   cudaGraph_t graph = nullptr;
   e = cudaStreamEndCapture(ctx->stream, &graph);
   ctx->timing = timing;
@@ -895,7 +857,7 @@ extern "C" ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npair
       }
     for (int k = 0; k < std::max(1, reps) && !s; ++k) {
       s = ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, smp, dist, nrm, nullptr,
-                  kModeGjkEpa, nullptr, pool->acc());
+                  kModeGjkEpa);
       if (s) break;
       const char* names[ogx_ctx::kMaxTimed];
       float ms[ogx_ctx::kMaxTimed];

@@ -68,12 +68,6 @@ struct ogx_pool {
   ogx::BodyRef* d_bodies = nullptr;
   int64_t* d_voff = nullptr;  // first point of each body in the AoS source
   std::vector<int64_t> h_voff;  // the same on the host (chunked uploads)
-  // bins of the large bodies for bounded support scans (built with every load)
-  ogx::AccRef* d_acc = nullptr;
-  float4* d_acc_bins = nullptr;
-  uint16_t* d_acc_idx = nullptr;
-  int nacc = 0;
-  ogx::PoolAcc acc() const { return ogx::PoolAcc{nacc ? d_acc : nullptr, d_acc_bins, d_acc_idx}; }
 };
 
 ogx_status ogx_fail(ogx_status s, const char* fmt, ...);
@@ -81,7 +75,4 @@ ogx_status ogx_cuda_fail(cudaError_t e, const char* what);
 ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos);
 ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const ogx::BodyRef* d_bodies, int nbodies,
                    int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
-                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm = nullptr,
-                   ogx::PoolAcc acc = ogx::PoolAcc{nullptr, nullptr, nullptr});
-ogx_status pool_pack_range(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos, int b0, int b1,
-                           cudaStream_t st);
+                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm = nullptr);

@@ -24,106 +24,6 @@ __global__ void k_pack(const float* __restrict__ aos, const int64_t* __restrict_
 }
 
 // ---------------------------------------------------------------------------------
-// bins of the large bodies (see MemBodies::scan_bins): one warp per body
-
-__device__ __forceinline__ int ord_key(float f) {
-  const int i = __float_as_int(f);
-  return i >= 0 ? i : i ^ 0x7fffffff;
-}
-__device__ __forceinline__ float ord_val(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
-
-__device__ __forceinline__ int acc_bin(float qx, float qy, float qz) {
-  const int oct = (qx < 0.0f ? 1 : 0) | (qy < 0.0f ? 2 : 0) | (qz < 0.0f ? 4 : 0);
-  const float ax = fabsf(qx), ay = fabsf(qy), az = fabsf(qz);
-  const int dom = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
-  return oct * 3 + dom;
-}
-
-__global__ void __launch_bounds__(128) k_accel(const float* __restrict__ pool, const BodyRef* __restrict__ bodies,
-                                               const AccRef* __restrict__ refs, int nbodies, float4* __restrict__ bins,
-                                               uint16_t* __restrict__ idx) {
-  __shared__ int s_cnt[4][kAccBins], s_cur[4][kAccBins];
-  __shared__ int s_lo[4][kAccBins][3], s_hi[4][kAccBins][3];
-  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int b = warp; b < nbodies; b += nwarps) {
-    const AccRef r = refs[b];
-    if (r.bins < 0) continue;
-    const BodyRef br = bodies[b];
-    const int n = br.n, n4 = round4(n);
-    const float* X = pool + 4 * (size_t)br.quad;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    for (int i = lane; i < n; i += 32) {
-      sx += X[i];
-      sy += X[n4 + i];
-      sz += X[2 * n4 + i];
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-      sz += __shfl_xor_sync(0xffffffffu, sz, o);
-    }
-    const float cx = sx / n, cy = sy / n, cz = sz / n;
-    if (lane < kAccBins) {
-      s_cnt[wl][lane] = 0;
-      for (int k = 0; k < 3; ++k) {
-        s_lo[wl][lane][k] = 0x7fffffff;
-        s_hi[wl][lane][k] = (int)0x80000000;
-      }
-    }
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
-      const float x = X[i], y = X[n4 + i], z = X[2 * n4 + i];
-      const int bin = acc_bin(x - cx, y - cy, z - cz);
-      atomicAdd(&s_cnt[wl][bin], 1);
-      atomicMin(&s_lo[wl][bin][0], ord_key(x));
-      atomicMin(&s_lo[wl][bin][1], ord_key(y));
-      atomicMin(&s_lo[wl][bin][2], ord_key(z));
-      atomicMax(&s_hi[wl][bin][0], ord_key(x));
-      atomicMax(&s_hi[wl][bin][1], ord_key(y));
-      atomicMax(&s_hi[wl][bin][2], ord_key(z));
-    }
-    __syncwarp();
-    const int c = lane < kAccBins ? s_cnt[wl][lane] : 0;
-    int inc = c;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += y;
-    }
-    const int start = inc - c;
-    if (lane < kAccBins) s_cur[wl][lane] = start;
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
-      const int bin = acc_bin(X[i] - cx, X[n4 + i] - cy, X[2 * n4 + i] - cz);
-      const int pos = atomicAdd(&s_cur[wl][bin], 1);
-      idx[r.idx + pos] = (uint16_t)i;
-    }
-    if (lane < kAccBins) {
-      float4 lo, hi;
-      lo.x = ord_val(s_lo[wl][lane][0]);
-      lo.y = ord_val(s_lo[wl][lane][1]);
-      lo.z = ord_val(s_lo[wl][lane][2]);
-      lo.w = __int_as_float(start);
-      hi.x = ord_val(s_hi[wl][lane][0]);
-      hi.y = ord_val(s_hi[wl][lane][1]);
-      hi.z = ord_val(s_hi[wl][lane][2]);
-      hi.w = __int_as_float(c);
-      bins[2 * (size_t)(r.bins + lane)] = lo;
-      bins[2 * (size_t)(r.bins + lane) + 1] = hi;
-    }
-    __syncwarp();
-  }
-}
-
-cudaError_t launch_accel(const float* pool, const BodyRef* bodies, const AccRef* refs, int nbodies, float4* bins,
-                         uint16_t* idx, int grid, cudaStream_t st) {
-  if (nbodies <= 0) return cudaSuccess;
-  k_accel<<<grid, 128, 0, st>>>(pool, bodies, refs, nbodies, bins, idx);
-  return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------------
 __device__ __forceinline__ bool pair_ok(const DevBatch& B, int2 pr) {
   return pr.x >= 0 && pr.x < B.nbodies && pr.y >= 0 && pr.y < B.nbodies;
 }

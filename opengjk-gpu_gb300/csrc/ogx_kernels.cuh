@@ -58,13 +58,6 @@ constexpr int kCntSlots = 2 * kBuckets + 5;
 constexpr int kRefineLaneMax = 128;
 constexpr int kRefineIters = 16;
 
-// bins of a pool's large bodies (see MemBodies::scan_bins); refs null: none
-struct PoolAcc {
-  const AccRef* refs;
-  const float4* bins;
-  const uint16_t* idx;
-};
-
 struct DevBatch {
   const float* pool;
   const BodyRef* bodies;
@@ -84,10 +77,6 @@ struct DevBatch {
                       // (small bodies from the front, large ones from the back)
   int* spill;         // npairs entries: contacts to re-run at full EPA capacity
   const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
-  // optional bins of the large bodies (bounded support scans); refs null: full scans
-  const AccRef* acc_refs;
-  const float4* acc_bins;
-  const uint16_t* acc_idx;
   ogx_config cfg;
   int mode;
 };
@@ -169,18 +158,6 @@ __device__ __forceinline__ void bind_src(MemBodies& s, const float* pool, BodyRe
   s.bind(pool, a, b);
 }
 
-// the bodies of pair pr, with the pool's bins for memory scans when it has them
-template <int L, class Src>
-__device__ __forceinline__ void bind_pair(Src& s, const DevBatch& B, int2 pr, BodyRef a, BodyRef b, int lane) {
-  bind_src<L>(s, B.pool, a, b, lane);
-}
-template <int L>
-__device__ __forceinline__ void bind_pair(MemBodies& s, const DevBatch& B, int2 pr, BodyRef a, BodyRef b,
-                                          int lane) {
-  s.bind(B.pool, a, b);
-  if (B.acc_refs) s.bind_acc(B.acc_bins, B.acc_idx, B.acc_refs[pr.x], B.acc_refs[pr.y]);
-}
-
 // Store one finished pair's GJK result and route it (EPA list, FP64 refinement list).
 __device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, const GjkState& g, bool lead) {
   const bool contact = gjk_contact(g);
@@ -217,7 +194,7 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
     typename SrcOf<L, K>::type src;
-    bind_pair<L>(src, B, pr, ra, rb, t.lane());
+    bind_src<L>(src, B.pool, ra, rb, t.lane());
     int2 ws = make_int2(0, 0);
     if (B.warm) {
       ws = B.warm[p];
@@ -237,7 +214,7 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
                                          Mem& M, bool can_spill, bool* spill64 = nullptr) {
   const int2 pr = B.pairs[p];
   typename SrcOf<L, K>::type src;
-  bind_pair<L>(src, B, pr, B.bodies[pr.x], B.bodies[pr.y], t.lane());
+  bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
   GjkState g;
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
@@ -330,8 +307,6 @@ cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream
 cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st);
 cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);
-cudaError_t launch_accel(const float* pool, const BodyRef* bodies, const AccRef* refs, int nbodies,
-                         float4* bins, uint16_t* idx, int grid, cudaStream_t st);
 cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st);
 cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st);

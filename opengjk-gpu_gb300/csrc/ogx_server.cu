@@ -191,8 +191,6 @@ struct ogx_server {
   ogx_ctx* pctx = nullptr;  // owns the local pool and the transform stream
   ogx_pool* local = nullptr;
   std::vector<float*> d_world;
-  std::vector<float4*> d_wbins;   // bins of each world copy's large bodies
-  std::vector<uint16_t*> d_widx;
   std::vector<float*> d_xf;
   std::vector<float*> h_xf;
   std::vector<int64_t> world_version;
@@ -289,9 +287,8 @@ bool ogx_server::launch_narrow(Request* r, Slot& s, int w) {
     r->err = ogx_cuda_fail(e, "server request launch");
     return false;
   }
-  const PoolAcc acc{local->nacc ? local->d_acc : nullptr, d_wbins[w], d_widx[w]};
   ogx_status os = n > 0 ? ogx_run(s.ctx, d_world[w], local->d_bodies, local->nbodies, n, s.d_pairs, s.d_smp, s.d_dist,
-                                  s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr, acc)
+                                  s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr)
                         : OGX_OK;
   if (os) {
     r->err = os;
@@ -450,10 +447,6 @@ void ogx_server::release() {
   }
   slots.clear();
   for (float* p : d_world) cudaFree(p);
-  for (float4* p : d_wbins) cudaFree(p);
-  for (uint16_t* p : d_widx) cudaFree(p);
-  d_wbins.clear();
-  d_widx.clear();
   for (float* p : d_xf) cudaFree(p);
   for (float* p : h_xf) cudaFreeHost(p);
   for (cudaEvent_t e : world_ready)
@@ -515,18 +508,6 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
         (e = halloc(&hx, 12 * (size_t)num_bodies)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
       st = ogx_cuda_fail(e, "server world buffers");
-    float4* wb = nullptr;
-    uint16_t* wi = nullptr;
-    if (!st && S->local->nacc > 0) {
-      int64_t pts = 0;
-      for (int b = 0; b < num_bodies; ++b)
-        if (counts[b] >= kAccMin && counts[b] <= kAccMax) pts += counts[b];
-      if ((e = dalloc(&wb, (size_t)S->local->nacc * kAccBins * 2)) != cudaSuccess ||
-          (e = dalloc(&wi, (size_t)std::max<int64_t>(8, pts))) != cudaSuccess)
-        st = ogx_cuda_fail(e, "server world bins");
-    }
-    S->d_wbins.push_back(wb);
-    S->d_widx.push_back(wi);
     S->d_world.push_back(dw);
     S->d_xf.push_back(dx);
     S->h_xf.push_back(hx);
@@ -625,9 +606,6 @@ extern "C" ogx_status ogx_server_set_transforms(ogx_server* S, const float* xf, 
                                                                      S->local->nbodies, S->d_xf[w], S->d_world[w]);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess && S->local->nacc > 0)
-    e = launch_accel(S->d_world[w], S->local->d_bodies, S->local->d_acc, S->local->nbodies, S->d_wbins[w],
-                     S->d_widx[w], 8 * S->pctx->sm_count, S->pctx->stream);
   if (e == cudaSuccess) e = cudaEventRecord(S->world_ready[w], S->pctx->stream);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "server transform");
   S->world_version[w] = v;

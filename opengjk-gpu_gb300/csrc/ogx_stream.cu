@@ -132,9 +132,11 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
     kneed = std::min(std::max(kneed, 0), C - 1);
     while (packed <= kneed) {
       e = cudaStreamWaitEvent(ctx->stream, ev_body[packed], 0);
-      if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed wait");
-      s = pool_pack_range(ctx, pool, d_aos, bb[packed], bb[packed + 1], ctx->stream);
-      if (s) return s;
+      const int n = bb[packed + 1] - bb[packed];
+      if (e == cudaSuccess && n > 0)
+        e = launch_pack(d_aos, pool->d_voff + bb[packed], pool->d_bodies + bb[packed], n, pool->d_points,
+                        std::max(1, std::min(8 * ctx->sm_count, (n + 7) / 8)), ctx->stream);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
       ++launches;
       ++packed;
     }
@@ -143,8 +145,7 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
     const int p0 = pb[j], n = pb[j + 1] - pb[j];
     if (n > 0) {
       s = ogx_run(ctx, pool->d_points, pool->d_bodies, nb, n, ctx->d_io_pairs + p0, ctx->d_io_smp + p0,
-                  ctx->d_io_dist + p0, ctx->d_io_nrm + 3 * (size_t)p0, ctx->d_io_status + p0, kModeGjkEpa,
-                  nullptr, pool->acc());
+                  ctx->d_io_dist + p0, ctx->d_io_nrm + 3 * (size_t)p0, ctx->d_io_status + p0, kModeGjkEpa);
       if (s) return s;
       launches += ctx->last_launches;
     }
@@ -168,9 +169,11 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
   // bodies never referenced are still packed, so the pool holds the whole upload
   while (packed < C) {
     e = cudaStreamWaitEvent(ctx->stream, ev_body[packed], 0);
-    if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed wait");
-    s = pool_pack_range(ctx, pool, d_aos, bb[packed], bb[packed + 1], ctx->stream);
-    if (s) return s;
+    const int n = bb[packed + 1] - bb[packed];
+    if (e == cudaSuccess && n > 0)
+      e = launch_pack(d_aos, pool->d_voff + bb[packed], pool->d_bodies + bb[packed], n, pool->d_points,
+                      std::max(1, std::min(8 * ctx->sm_count, (n + 7) / 8)), ctx->stream);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
     ++launches;
     ++packed;
   }
