@@ -102,6 +102,7 @@ constexpr int kBucketCap[kBuckets] = {16, 32, 64, 128, 256, 512, 0};
 std::mutex g_init_mu;
 int g_init_device = -1;
 int g_grid_bin = 0, g_grid_polish = 0, g_grid_pack = 0, g_grid_refine = 0, g_grid_spill = 0;
+uint32_t* g_subtab = nullptr;  // sub-distance decision table on the initialised device
 // per-device autotuned choices (variant index per bucket), -1 = not tuned
 int g_tuned[16][2][kBuckets];
 bool g_tuned_valid[16];
@@ -197,6 +198,15 @@ ogx_status init_kernels(int device) {
   e = refine_occupancy(kBlock, &per_sm);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy(k_refine)");
   g_grid_refine = std::max(1, per_sm) * sms;
+  {
+    std::vector<uint32_t> tab(kSubTabSize);
+    fill_subtab(tab.data());
+    if (g_subtab) cudaFree(g_subtab);
+    g_subtab = nullptr;
+    if ((e = cudaMalloc(&g_subtab, kSubTabSize * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemcpy(g_subtab, tab.data(), kSubTabSize * sizeof(uint32_t), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return ogx_cuda_fail(e, "decision table");
+  }
   g_init_device = device;
   return OGX_OK;
 }
@@ -609,6 +619,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.refine_full = ctx->d_refine_full;
   B.spill = ctx->d_spill;
   B.warm = d_warm;
+  B.subtab = g_subtab;
   B.cfg = ctx->cfg;
   B.mode = mode;
   cudaStream_t st = ctx->stream;

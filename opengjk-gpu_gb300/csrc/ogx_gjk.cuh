@@ -564,7 +564,8 @@ OGX_HD void gjk_start(const Bodies& B, GjkRun& r, int start_a = 0, int start_b =
 }
 
 template <class Team, class Bodies>
-OGX_HD void gjk_iterate(const Team& t, const Bodies& B, const Config& cfg, GjkRun& r) {
+OGX_HD void gjk_iterate(const Team& t, const Bodies& B, const Config& cfg, GjkRun& r,
+                        const uint32_t* subtab = nullptr) {
   const bool reftol = (cfg.flags & OGX_F_REFERENCE_TOL) != 0;
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
   const float eps_rel2 = cfg.gjk_eps_rel * cfg.gjk_eps_rel;
@@ -642,7 +643,14 @@ OGX_HD void gjk_iterate(const Team& t, const Bodies& B, const Config& cfg, GjkRu
     StepIn S;
     uint32_t bits, unc;
     step_predicates(n, P, S, bits, unc);
-    SubOut o = step_decide(n, bits);
+    // the decision: one load from the table on the device, the tree on the host
+    SubOut o;
+#if defined(__CUDA_ARCH__)
+    if (subtab)
+      o = unpack_subout(__ldg(subtab + subtab_index(n, bits)));
+    else
+#endif
+      o = step_decide(n, bits);
     // degenerate spans make the projection itself unreliable
     if (o.kind == SO_LINE) {
       const float ge = o.a == 0 ? S.g[0][0] : (o.a == 1 ? S.g[1][1] : S.g[2][2]);
@@ -799,10 +807,10 @@ OGX_HD void gjk_end(const Team& t, const Bodies& B, const Config& cfg, const Gjk
 
 template <class Team, class Bodies>
 OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState& g, int start_a = 0,
-                     int start_b = 0) {
+                     int start_b = 0, const uint32_t* subtab = nullptr) {
   GjkRun r;
   gjk_start(B, r, start_a, start_b);
-  while (!r.done) gjk_iterate(t, B, cfg, r);
+  while (!r.done) gjk_iterate(t, B, cfg, r, subtab);
   gjk_end(t, B, cfg, r, g);
 }
 

@@ -77,6 +77,7 @@ struct DevBatch {
                       // (small bodies from the front, large ones from the back)
   int* spill;         // npairs entries: contacts to re-run at full EPA capacity
   const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
+  const uint32_t* subtab;  // sub-distance decision table (fill_subtab); null: the tree
   ogx_config cfg;
   int mode;
 };
@@ -201,7 +202,7 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
       if (ws.x < 0 || ws.x >= ra.n || ws.y < 0 || ws.y >= rb.n) ws = make_int2(0, 0);
     }
     GjkState g;
-    gjk_pair(t, src, B.cfg, g, ws.x, ws.y);
+    gjk_pair(t, src, B.cfg, g, ws.x, ws.y, B.subtab);
     gjk_store(B, bucket, p, g, t.lane() == 0);
   }
 }

@@ -172,6 +172,7 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
   B.polish = reinterpret_cast<PolishRec*>(S->scratch + kOffPolish);
   B.spill = reinterpret_cast<int*>(S->scratch + kOffSpill);
   B.warm = nullptr;
+  B.subtab = nullptr;  // the decision tree (same outcomes as the engine's table)
   B.cfg = c;
   B.mode = kModeGjkEpa;
 

@@ -183,6 +183,40 @@ OGX_HD SubOut tetra_tree(Bits& B) {
 }
 
 // ------------------------------------------------------------------------------
+// The decision as a table: every outcome of step_decide packed in 32 bits, indexed by
+// the predicate bits the decision can read (13 for a tetrahedron step, 4 for a triangle,
+// 1 for a segment).  One load replaces the branches of the tree, which the lanes of a
+// warp (different pairs, different bits) would otherwise take one path after another.
+constexpr int kSubTab3 = 1 << 13;           // first triangle entry
+constexpr int kSubTab2 = kSubTab3 + 16;     // first segment entry
+constexpr int kSubTabSize = kSubTab2 + 2;
+
+OGX_HD int subtab_index(int n, uint32_t bits) {
+  if (n == 4) return (int)(bits & 0x1fffu);
+  if (n == 3)
+    return kSubTab3 + (int)((bits & 3u) | (((bits >> (PB_D + 0)) & 1u) << 2) | (((bits >> (PB_D + 1)) & 1u) << 3));
+  return kSubTab2 + (int)(bits & 1u);
+}
+
+// n-1 (2 bits) | s0, s1, s2 (2 bits each) | kind (3) | a, b (2 each) | used (13)
+OGX_HD uint32_t pack_subout(const SubOut& o) {
+  return (uint32_t)(o.n - 1) | ((uint32_t)o.s[0] << 2) | ((uint32_t)o.s[1] << 4) | ((uint32_t)o.s[2] << 6) |
+         ((uint32_t)o.kind << 8) | ((uint32_t)o.a << 11) | ((uint32_t)o.b << 13) | ((o.used & 0x1fffu) << 15);
+}
+OGX_HD SubOut unpack_subout(uint32_t c) {
+  SubOut o;
+  o.n = (int)(c & 3u) + 1;
+  o.s[0] = (int)((c >> 2) & 3u);
+  o.s[1] = (int)((c >> 4) & 3u);
+  o.s[2] = (int)((c >> 6) & 3u);
+  o.kind = (int)((c >> 8) & 7u);
+  o.a = (int)((c >> 11) & 3u);
+  o.b = (int)((c >> 13) & 3u);
+  o.used = (c >> 15) & 0x1fffu;
+  return o;
+}
+
+// ------------------------------------------------------------------------------
 // FP32 predicate values and bounds
 
 struct StepIn {
@@ -274,6 +308,16 @@ OGX_HD SubOut step_decide(int n, uint32_t bits) {
   }
   o.used = B.used;
   return o;
+}
+
+// the whole table (host): entry i is step_decide of the bits that index i
+inline void fill_subtab(uint32_t* tab) {
+  for (uint32_t bits = 0; bits < (1u << 13); ++bits) tab[bits] = pack_subout(step_decide(4, bits));
+  for (uint32_t k = 0; k < 16; ++k) {
+    const uint32_t bits = (k & 3u) | (((k >> 2) & 1u) << (PB_D + 0)) | (((k >> 3) & 1u) << (PB_D + 1));
+    tab[kSubTab3 + k] = pack_subout(step_decide(3, bits));
+  }
+  for (uint32_t k = 0; k < 2; ++k) tab[kSubTab2 + k] = pack_subout(step_decide(2, k));
 }
 
 // new direction v from the outcome (all candidates computed, then selected)
