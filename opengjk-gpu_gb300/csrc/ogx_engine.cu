@@ -669,7 +669,12 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   }
   if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
     ctx->mark("refine");
-    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st);
+    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st,
+                      fork ? ctx->aux[0] : st, fork ? ctx->fork_ev : nullptr);
+    if (e == cudaSuccess && fork) {
+      e = cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->join_ev[0], 0);
+    }
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
     launches += 3;
   }

@@ -295,10 +295,19 @@ cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st) {
+// k_refine routes the continuations; the two continuation kernels are independent and
+// run on st and st2 (the same stream when st2 == st; the caller joins st2 back)
+cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st, cudaStream_t st2,
+                          cudaEvent_t routed) {
   k_refine<<<grid, 128, 0, st>>>(B);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && st2 != st) {
+    e = cudaEventRecord(routed, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, routed, 0);
+  }
+  if (e != cudaSuccess) return e;
   k_refine_lane<<<grid, 128, 0, st>>>(B);
-  k_refine_full<<<grid_full, 128, 0, st>>>(B);
+  k_refine_full<<<grid_full, 128, 0, st2>>>(B);
   return cudaGetLastError();
 }
 

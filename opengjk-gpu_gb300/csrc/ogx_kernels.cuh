@@ -304,7 +304,8 @@ int epa_variants_b(const KernelInfo** out);
 int epa_variants_c(const KernelInfo** out);
 
 // non-template kernels (ogx_k_misc.cu)
-cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st);
+cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st, cudaStream_t st2,
+                          cudaEvent_t routed);
 cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st);
 cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);

@@ -184,7 +184,7 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
     S->gjk[b].fn<<<S->grid_gjk[b], kNoAllocBlock, 0, s>>>(B, b);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess && (c.flags & OGX_F_FP64_POLISH)) e = launch_refine(B, S->grid_refine, S->grid_bin, s);
+  if (e == cudaSuccess && (c.flags & OGX_F_FP64_POLISH)) e = launch_refine(B, S->grid_refine, S->grid_bin, s, s, nullptr);
   for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
     S->epa[b].fn<<<S->grid_epa[b], kNoAllocBlock, S->smem_epa[b], s>>>(B, b);
     e = cudaGetLastError();
