@@ -242,6 +242,12 @@ ogx_status ogx_contact_response(ogx_ctx* ctx, int num_bodies, const ogx_body_sta
                                 const gkSimplex* d_simplices, const ogx_response_params* params,
                                 float* d_vel_out, float* d_ang_out, float* d_pos_out);
 
+/* Timeline of the last ogx_gjk_epa_streamed call made with timing on
+ * (ogx_ctx_set_timing): 5 values per chunk, ms from the call's start: end of its body
+ * upload, end of its pair upload, start and end of its kernels, end of its download.
+ * Returns the number of values (writes at most cap). */
+int ogx_ctx_stream_timeline(const ogx_ctx* ctx, float* ms, int cap);
+
 /* CUDA graph of one call: captures the launches of ogx_gjk / ogx_gjk_epa / ogx_epa
  * (mode 1 / 2 / 3) on these buffers once; ogx_graph_launch replays them on the context's
  * stream with one launch.  The buffers' contents may change between launches, their

@@ -53,6 +53,7 @@ struct ogx_ctx {
   float* d_io_nrm = nullptr;
   int32_t* d_io_status = nullptr;
   size_t io_cap = 0;
+  std::vector<float> stream_timeline;  // last streamed call with timing on (see ogx.h)
 
   ogx_status ensure_scratch(int npairs);
   ogx_status ensure_stage(size_t host_bytes, size_t dev_bytes);

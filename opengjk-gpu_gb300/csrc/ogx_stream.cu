@@ -101,6 +101,20 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
       });
     for (auto& t : th) t.join();
   }
+  // optional timeline (context timing on): per chunk, the end of its body upload, the end
+  // of its pair upload, its compute start and end, the end of its download
+  const bool tl = ctx->timing;
+  std::vector<cudaEvent_t> tev;
+  if (tl) {
+    tev.resize(1 + 5 * C);
+    for (auto& x : tev) cudaEventCreate(&x);
+    cudaEventRecord(tev[0], ctx->up);
+    cudaStreamWaitEvent(ctx->stream, tev[0], 0);
+    cudaStreamWaitEvent(ctx->down, tev[0], 0);
+  }
+  auto mark = [&](int j, int k, cudaStream_t s2) {
+    if (tl) cudaEventRecord(tev[1 + 5 * j + k], s2);
+  };
   cudaEvent_t* ev_body = ctx->sev.data();
   cudaEvent_t* ev_pair = ev_body + C;
   cudaEvent_t* ev_done = ev_pair + C;
@@ -114,10 +128,12 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
       e = cudaMemcpyAsync(const_cast<float*>(d_aos) + 3 * p0, xyz + 3 * p0, (p1 - p0) * 3 * sizeof(float),
                           cudaMemcpyHostToDevice, ctx->up);
     if (e == cudaSuccess) e = cudaEventRecord(ev_body[k], ctx->up);
+    mark(k, 0, ctx->up);
     if (e == cudaSuccess && pb[k + 1] > pb[k])
       e = cudaMemcpyAsync(ctx->d_io_pairs + pb[k], pairs + pb[k], (pb[k + 1] - pb[k]) * sizeof(gkCollisionPair),
                           cudaMemcpyHostToDevice, ctx->up);
     if (e == cudaSuccess) e = cudaEventRecord(ev_pair[k], ctx->up);
+    mark(k, 1, ctx->up);
   }
   if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed upload");
   // compute: pack body ranges on first use, then the pair range
@@ -142,6 +158,7 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
     }
     e = cudaStreamWaitEvent(ctx->stream, ev_pair[j], 0);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed wait");
+    mark(j, 2, ctx->stream);
     const int p0 = pb[j], n = pb[j + 1] - pb[j];
     if (n > 0) {
       s = ogx_run(ctx, pool->d_points, pool->d_bodies, nb, n, ctx->d_io_pairs + p0, ctx->d_io_smp + p0,
@@ -149,6 +166,7 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
       if (s) return s;
       launches += ctx->last_launches;
     }
+    mark(j, 3, ctx->stream);
     e = cudaEventRecord(ev_done[j], ctx->stream);
     // results of range j
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->down, ev_done[j], 0);
@@ -165,6 +183,7 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
       e = cudaMemcpyAsync(status + p0, ctx->d_io_status + p0, n * sizeof(int32_t), cudaMemcpyDeviceToHost,
                           ctx->down);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed download");
+    mark(j, 4, ctx->down);
   }
   // bodies never referenced are still packed, so the pool holds the whole upload
   while (packed < C) {
@@ -180,6 +199,18 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
   e = cudaStreamSynchronize(ctx->down);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed call");
+  if (tl) {
+    ctx->stream_timeline.assign(5 * C, 0.0f);
+    for (int i = 0; i < 5 * C; ++i) cudaEventElapsedTime(&ctx->stream_timeline[i], tev[0], tev[1 + i]);
+    for (auto& x : tev) cudaEventDestroy(x);
+  }
   ctx->last_launches = launches;
   return OGX_OK;
+}
+
+extern "C" int ogx_ctx_stream_timeline(const ogx_ctx* ctx, float* ms, int cap) {
+  if (!ctx) return 0;
+  const int n = (int)ctx->stream_timeline.size();
+  if (ms) for (int i = 0; i < n && i < cap; ++i) ms[i] = ctx->stream_timeline[i];
+  return n;
 }

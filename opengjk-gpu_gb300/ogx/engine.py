@@ -332,6 +332,15 @@ def reduce_submesh_pairs(ctx: Context, offsets_dev, sub_dist_dev, max_sub_pairs:
     return best[:n], arg[:n]
 
 
+def stream_timeline(ctx: Context) -> np.ndarray:
+    """[chunks, 5] ms of the last streamed call made with timing on: body upload end, pair
+    upload end, kernels start, kernels end, download end."""
+    n = ctx.lib.ogx_ctx_stream_timeline(ctx.handle, None, 0)
+    buf = (ctypes.c_float * max(n, 1))()
+    ctx.lib.ogx_ctx_stream_timeline(ctx.handle, buf, n)
+    return np.array(buf[:n], np.float32).reshape(-1, 5)
+
+
 class Graph:
     """One call captured as a CUDA graph (ogx_graph_*): `launch()` replays the whole
     pipeline on the context's stream with one launch.  The pair and output buffers are
