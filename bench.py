@@ -24,6 +24,10 @@ import sys
 import threading
 import time
 
+# more hardware work queues than the runtime's default 8, so that the streamed call's
+# lanes and their per-bucket streams do not serialise (read when CUDA starts)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "opengjk-gpu_gb300"))
 sys.path.insert(0, ROOT)
@@ -53,7 +57,7 @@ def parse():
     ap.add_argument("--choice", default="",
                     help='kernel variants instead of autotuning, as printed in "kernel_choice" (JSON)')
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
-    ap.add_argument("--chunks", type=int, default=4, help="pieces of the end-to-end streamed call")
+    ap.add_argument("--chunks", type=int, default=8, help="pieces of the end-to-end streamed call")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
     return ap.parse_args()

@@ -191,6 +191,18 @@ ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, 
                                 const gkCollisionPair* pairs, gkSimplex* simplices,
                                 float* distances, float* normals, int32_t* status, int chunks);
 
+/* ogx_gjk_epa_streamed with the caller's pieces: pair range j is
+ * [pair_bounds[j], pair_bounds[j + 1]) (nranges + 1 non-decreasing bounds from 0 to
+ * npairs, 1 <= nranges <= 64), and up to `lanes` ranges compute side by side
+ * (1..8; 0 = the default, 4).  Body range j goes up with pair range j and holds the
+ * bodies that pair range j is the first to reference, so pairs listed in body order
+ * start computing early.  ogx_gjk_epa_streamed(..., chunks) is this call with
+ * `chunks` equal ranges. */
+ogx_status ogx_gjk_epa_streamed_ranges(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
+                                       const gkCollisionPair* pairs, gkSimplex* simplices,
+                                       float* distances, float* normals, int32_t* status,
+                                       const int* pair_bounds, int nranges, int lanes);
+
 /* Bodies made of several convex parts (a convex decomposition; parts are the pool's
  * bodies, body B owns parts [first[B], first[B] + count[B])).  Expansion of body pairs
  * into part pairs, as the reference's visualiser does it

@@ -306,6 +306,7 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
     cudaStreamDestroy(ctx->down);
   }
   for (cudaEvent_t e : ctx->sev) cudaEventDestroy(e);
+  for (ogx_ctx* c : ctx->sub) ogx_ctx_destroy(c);
   for (int b = 0; b < kBuckets; ++b) {
     if (ctx->aux[b]) {
       cudaStreamSynchronize(ctx->aux[b]);
@@ -639,7 +640,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   // The seven bucket kernels of a stage run concurrently (one stream each, forked from
   // and joined back into the context's stream) so that the tail of one bucket overlaps
   // the others' work; with per-kernel timing on they run in sequence.
-  const bool fork = !ctx->timing && ctx->ensure_aux() == OGX_OK;
+  const bool fork = !ctx->timing && ctx->fork_ok && ctx->ensure_aux() == OGX_OK;
   auto bucket_stream = [&](int b) -> cudaStream_t { return fork ? ctx->aux[b] : st; };
   auto fork_out = [&]() -> cudaError_t {
     if (!fork) return cudaSuccess;

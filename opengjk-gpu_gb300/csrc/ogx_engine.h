@@ -40,6 +40,7 @@ struct ogx_ctx {
 
   void mark(const char* name);  // record an event before the next launch
   // concurrent bucket launches: one stream per size bucket, fork / join events
+  bool fork_ok = true;
   cudaStream_t aux[ogx::kBuckets] = {};
   cudaEvent_t fork_ev = nullptr;
   cudaEvent_t join_ev[ogx::kBuckets] = {};
@@ -54,6 +55,7 @@ struct ogx_ctx {
   int32_t* d_io_status = nullptr;
   size_t io_cap = 0;
   std::vector<float> stream_timeline;  // last streamed call with timing on (see ogx.h)
+  std::vector<ogx_ctx*> sub;           // streamed calls: contexts running chunks side by side
 
   ogx_status ensure_scratch(int npairs);
   ogx_status ensure_stage(size_t host_bytes, size_t dev_bytes);

@@ -1,16 +1,19 @@
 // ogx_stream.cu -- one GJK + EPA call from host memory to host memory with the transfers
 // overlapped with the kernels.
 //
-// The points of the pool go up in body ranges (copy engine, stream `up`), the pairs in
-// ranges of pairs; chunk j of the pairs starts (context stream) as soon as every body it
-// references and its pairs are on the device, after packing the new body ranges into the
-// pool layout; its results come back (stream `down`) while later chunks compute.  The
+// The pairs go up in C ranges of equal size and the points in C body ranges cut so that
+// range k holds the bodies pair range k references first (copy engine, stream `up`).
+// Each body range is packed into the pool layout on the context's stream as it lands;
+// chunk j of the pairs then runs on one of up to four lane contexts (own stream and work
+// lists), so that chunks overlap one another as well as the copies, and its results come
+// back (stream `down`) while later chunks compute.  The
 // reference's high-level functions copy everything, compute, and copy back in sequence
 // (GJK/gpu/openGJK.cu:2791-2819); here only the first chunk's upload and the last chunk's
 // download are exposed.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <thread>
 #include <vector>
 
@@ -46,6 +49,19 @@ ogx_status ensure_io(ogx_ctx* c, size_t n) {
   return OGX_OK;
 }
 
+// packs bodies [b0, b1) of the uploaded xyz into the pool layout
+cudaError_t pack_range(const ogx_ctx* ctx, ogx_pool* pool, const float* d_aos, int b0, int b1, cudaStream_t st) {
+  const int n = b1 - b0;
+  if (n <= 0) return cudaSuccess;
+  return launch_pack(d_aos, pool->d_voff + b0, pool->d_bodies + b0, n, pool->d_points,
+                     std::max(1, std::min(8 * ctx->sm_count, (n + 7) / 8)), st);
+}
+
+constexpr int kStreamMaxRanges = 64;
+constexpr int kStreamMaxLanes = 8;
+constexpr int kStreamLanes = 4;
+constexpr int kLaneForkConnections = 16;
+
 ogx_status ensure_streams(ogx_ctx* c, int nev) {
   cudaError_t e;
   if (!c->up && (e = cudaStreamCreateWithFlags(&c->up, cudaStreamNonBlocking)) != cudaSuccess)
@@ -61,35 +77,42 @@ ogx_status ensure_streams(ogx_ctx* c, int nev) {
   return OGX_OK;
 }
 
-}  // namespace
-
-extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
-                                           const gkCollisionPair* pairs, gkSimplex* simplices, float* distances,
-                                           float* normals, int32_t* status, int chunks) {
-  if (!ctx || !pool || (!xyz && pool->npoints > 0) || (!pairs && npairs > 0) || npairs < 0)
-    return ogx_fail(OGX_ERR_INVALID, "bad streamed-call arguments");
-  if (npairs == 0) return OGX_OK;
-  if (!simplices || !distances || !normals) return ogx_fail(OGX_ERR_INVALID, "NULL output array");
+ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, const gkCollisionPair* pairs,
+                    gkSimplex* simplices, float* distances, float* normals, int32_t* status,
+                    const std::vector<int>& pb, int lanes) {
   cudaSetDevice(ctx->device);
-  const int C = std::max(1, std::min(chunks, 64));
+  const int C = (int)pb.size() - 1;
   const int nb = pool->nbodies;
+  int widest = 0;
+  for (int j = 0; j < C; ++j) widest = std::max(widest, pb[j + 1] - pb[j]);
   ogx_status s = ensure_io(ctx, npairs);
-  if (!s) s = ensure_streams(ctx, 3 * C);
+  if (!s) s = ensure_streams(ctx, 4 * C);
+  // chunks run side by side on `lanes` contexts (own stream and work lists each), so that
+  // one chunk's kernels overlap the next chunk's as well as the copies
+  const int S = std::min(C, lanes);
+  while (!s && (int)ctx->sub.size() < S) {
+    ogx_ctx* c = nullptr;
+    s = ogx_ctx_create(ctx->device, &ctx->cfg, nullptr, &c);
+    if (!s) ctx->sub.push_back(c);
+  }
+  // a lane also spreads its size buckets over streams of its own, when the process has
+  // enough hardware work queues for them; with the runtime's default of 8 the ~35 streams
+  // would share queues and serialise behind one another
+  const char* conn_env = std::getenv("CUDA_DEVICE_MAX_CONNECTIONS");
+  const bool lane_fork = conn_env && std::atoi(conn_env) >= kLaneForkConnections;
+  for (int i = 0; !s && i < S; ++i) {
+    ogx_ctx* c = ctx->sub[i];
+    c->cfg = ctx->cfg;
+    c->timing = false;
+    c->fork_ok = lane_fork;
+    for (int k = 0; k < 2; ++k)
+      for (int b = 0; b < kBuckets; ++b) c->choice[k][b] = ctx->choice[k][b];
+    s = c->ensure_scratch(widest);
+  }
   if (!s) s = ctx->ensure_stage(0, (size_t)pool->npoints * 3 * sizeof(float));
-  if (!s) s = ctx->ensure_scratch(npairs);
   if (s) return s;
 
-  // body ranges of about equal point counts
-  std::vector<int> bb(C + 1, nb);
-  bb[0] = 0;
-  for (int k = 1; k < C; ++k) {
-    const int64_t target = pool->npoints * k / C;
-    bb[k] = (int)(std::lower_bound(pool->h_voff.begin(), pool->h_voff.end(), target) - pool->h_voff.begin());
-    bb[k] = std::max(bb[k], bb[k - 1]);
-  }
-  // pair ranges of equal size and the highest body each references (host threads)
-  std::vector<int> pb(C + 1);
-  for (int j = 0; j <= C; ++j) pb[j] = (int)((int64_t)npairs * j / C);
+  // the highest body each pair range references (host threads)
   std::vector<int> need(C, -1);
   {
     std::vector<std::thread> th;
@@ -101,6 +124,11 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
       });
     for (auto& t : th) t.join();
   }
+  // body range k holds the bodies that pair range k references first: chunk k then waits
+  // only for body ranges 0..k (indices out of range need no body; the kernels flag them)
+  std::vector<int> bb(C + 1, nb);
+  bb[0] = 0;
+  for (int k = 0; k + 1 < C; ++k) bb[k + 1] = std::max(bb[k], std::min(nb, need[k] + 1));
   // optional timeline (context timing on): per chunk, the end of its body upload, the end
   // of its pair upload, its compute start and end, the end of its download
   const bool tl = ctx->timing;
@@ -118,6 +146,7 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
   cudaEvent_t* ev_body = ctx->sev.data();
   cudaEvent_t* ev_pair = ev_body + C;
   cudaEvent_t* ev_done = ev_pair + C;
+  cudaEvent_t* ev_packed = ev_done + C;
   const float* d_aos = static_cast<const float*>(ctx->d_stage);
   cudaError_t e = cudaSuccess;
   // uploads, interleaved so that pair range j follows the bodies it most likely needs
@@ -136,38 +165,32 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
     mark(k, 1, ctx->up);
   }
   if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed upload");
-  // compute: pack body ranges on first use, then the pair range
-  int packed = 0;  // body ranges [0, packed) are in the pool
+  // chunk j of the pairs runs on lane j % S once the bodies it needs are packed and its
+  // pairs are up
   int launches = 0;
   for (int j = 0; j < C; ++j) {
-    // body range holding the highest body this pair range references (invalid indices
-    // are flagged by the kernels; they need no body)
-    int kneed = 0;
-    if (need[j] >= nb) kneed = C - 1;
-    else if (need[j] >= 0) kneed = (int)(std::upper_bound(bb.begin(), bb.end(), need[j]) - bb.begin()) - 1;
-    kneed = std::min(std::max(kneed, 0), C - 1);
-    while (packed <= kneed) {
-      e = cudaStreamWaitEvent(ctx->stream, ev_body[packed], 0);
-      const int n = bb[packed + 1] - bb[packed];
-      if (e == cudaSuccess && n > 0)
-        e = launch_pack(d_aos, pool->d_voff + bb[packed], pool->d_bodies + bb[packed], n, pool->d_points,
-                        std::max(1, std::min(8 * ctx->sm_count, (n + 7) / 8)), ctx->stream);
-      if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
-      ++launches;
-      ++packed;
-    }
-    e = cudaStreamWaitEvent(ctx->stream, ev_pair[j], 0);
+    // body range j, packed in order on the context's stream: ranges 0..j then hold every
+    // body that pair range j references
+    e = cudaStreamWaitEvent(ctx->stream, ev_body[j], 0);
+    if (e == cudaSuccess) e = pack_range(ctx, pool, d_aos, bb[j], bb[j + 1], ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_packed[j], ctx->stream);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
+    launches += bb[j + 1] > bb[j];
+    ogx_ctx* c = ctx->sub[j % S];
+    cudaStream_t cs = c->stream;
+    e = cudaStreamWaitEvent(cs, ev_packed[j], 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_pair[j], 0);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed wait");
-    mark(j, 2, ctx->stream);
+    mark(j, 2, cs);
     const int p0 = pb[j], n = pb[j + 1] - pb[j];
     if (n > 0) {
-      s = ogx_run(ctx, pool->d_points, pool->d_bodies, nb, n, ctx->d_io_pairs + p0, ctx->d_io_smp + p0,
+      s = ogx_run(c, pool->d_points, pool->d_bodies, nb, n, ctx->d_io_pairs + p0, ctx->d_io_smp + p0,
                   ctx->d_io_dist + p0, ctx->d_io_nrm + 3 * (size_t)p0, ctx->d_io_status + p0, kModeGjkEpa);
       if (s) return s;
-      launches += ctx->last_launches;
+      launches += c->last_launches;
     }
-    mark(j, 3, ctx->stream);
-    e = cudaEventRecord(ev_done[j], ctx->stream);
+    mark(j, 3, cs);
+    e = cudaEventRecord(ev_done[j], cs);
     // results of range j
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->down, ev_done[j], 0);
     if (e == cudaSuccess && n > 0)
@@ -185,19 +208,9 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
     if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed download");
     mark(j, 4, ctx->down);
   }
-  // bodies never referenced are still packed, so the pool holds the whole upload
-  while (packed < C) {
-    e = cudaStreamWaitEvent(ctx->stream, ev_body[packed], 0);
-    const int n = bb[packed + 1] - bb[packed];
-    if (e == cudaSuccess && n > 0)
-      e = launch_pack(d_aos, pool->d_voff + bb[packed], pool->d_bodies + bb[packed], n, pool->d_points,
-                      std::max(1, std::min(8 * ctx->sm_count, (n + 7) / 8)), ctx->stream);
-    if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
-    ++launches;
-    ++packed;
-  }
   e = cudaStreamSynchronize(ctx->down);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  for (int i = 0; i < S && e == cudaSuccess; ++i) e = cudaStreamSynchronize(ctx->sub[i]->stream);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed call");
   if (tl) {
     ctx->stream_timeline.assign(5 * C, 0.0f);
@@ -206,6 +219,44 @@ extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const f
   }
   ctx->last_launches = launches;
   return OGX_OK;
+}
+
+ogx_status check_args(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, const gkCollisionPair* pairs,
+                      gkSimplex* simplices, float* distances, float* normals) {
+  if (!ctx || !pool || (!xyz && pool->npoints > 0) || (!pairs && npairs > 0) || npairs < 0)
+    return ogx_fail(OGX_ERR_INVALID, "bad streamed-call arguments");
+  if (npairs > 0 && (!simplices || !distances || !normals)) return ogx_fail(OGX_ERR_INVALID, "NULL output array");
+  return OGX_OK;
+}
+
+}  // namespace
+
+extern "C" ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
+                                           const gkCollisionPair* pairs, gkSimplex* simplices, float* distances,
+                                           float* normals, int32_t* status, int chunks) {
+  ogx_status s = check_args(ctx, pool, xyz, npairs, pairs, simplices, distances, normals);
+  if (s || npairs == 0) return s;
+  const int C = std::max(1, std::min(chunks, kStreamMaxRanges));
+  std::vector<int> pb(C + 1);
+  for (int j = 0; j <= C; ++j) pb[j] = (int)((int64_t)npairs * j / C);
+  return streamed(ctx, pool, xyz, npairs, pairs, simplices, distances, normals, status, pb, kStreamLanes);
+}
+
+extern "C" ogx_status ogx_gjk_epa_streamed_ranges(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
+                                                  const gkCollisionPair* pairs, gkSimplex* simplices,
+                                                  float* distances, float* normals, int32_t* status,
+                                                  const int* pair_bounds, int nranges, int lanes) {
+  ogx_status s = check_args(ctx, pool, xyz, npairs, pairs, simplices, distances, normals);
+  if (s) return s;
+  if (!pair_bounds || nranges < 1 || nranges > kStreamMaxRanges || lanes < 0 || lanes > kStreamMaxLanes)
+    return ogx_fail(OGX_ERR_INVALID, "bad pair ranges or lane count");
+  std::vector<int> pb(pair_bounds, pair_bounds + nranges + 1);
+  if (pb[0] != 0 || pb[nranges] != npairs) return ogx_fail(OGX_ERR_INVALID, "pair ranges must cover [0, npairs)");
+  for (int j = 0; j < nranges; ++j)
+    if (pb[j + 1] < pb[j]) return ogx_fail(OGX_ERR_INVALID, "pair range bounds must not decrease");
+  if (npairs == 0) return OGX_OK;
+  return streamed(ctx, pool, xyz, npairs, pairs, simplices, distances, normals, status, pb,
+                  lanes ? lanes : kStreamLanes);
 }
 
 extern "C" int ogx_ctx_stream_timeline(const ogx_ctx* ctx, float* ms, int cap) {

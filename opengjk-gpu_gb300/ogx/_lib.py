@@ -127,6 +127,7 @@ SIGNATURES = {
     "ogx_broadphase": (_I, [_P, _P, ctypes.c_float, ctypes.c_float, _I, _P, _P]),
     "ogx_broad_destroy": (_I, [_P]),
     "ogx_gjk_epa_streamed": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I]),
+    "ogx_gjk_epa_streamed_ranges": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _I, _I]),
     "ogx_ctx_stream_timeline": (_I, [_P, _P, _I]),
     "ogx_contact_response": (_I, [_P, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "ogx_expand_submesh_pairs": (_I, [_P, _I, _P, _I, _P, _P, _I, _P, _P, _P]),

@@ -249,11 +249,14 @@ def run(ctx: Context, pool: Pool, pairs_dev, mode: int = MODE_GJK_EPA, out: Resu
     return out
 
 
-def streamed(ctx: Context, pool: Pool, coords, pairs, out: dict | None = None, chunks: int = 8) -> dict:
+def streamed(ctx: Context, pool: Pool, coords, pairs, out: dict | None = None, chunks: int = 8,
+             bounds=None, lanes: int = 0) -> dict:
     """Host-to-host GJK + EPA (ogx_gjk_epa_streamed): uploads `coords` (all bodies' xyz)
     and `pairs` in chunks, overlapping the copies with the kernels; synchronous.
     coords / pairs: numpy arrays or pinned torch CPU tensors; `out`: dict of host arrays
-    (simplex, dist, normal, status) to fill, allocated if None."""
+    (simplex, dist, normal, status) to fill, allocated if None.  `bounds` (ascending pair
+    indices from 0 to n) gives the pieces explicitly (ogx_gjk_epa_streamed_ranges), with
+    up to `lanes` pieces computing side by side (0 = default)."""
     def ptr(x):
         return x.data_ptr() if hasattr(x, "data_ptr") else x.ctypes.data
     n = int(pairs.shape[0])
@@ -261,9 +264,13 @@ def streamed(ctx: Context, pool: Pool, coords, pairs, out: dict | None = None, c
         out = {"simplex": np.zeros(n, SIMPLEX_DTYPE), "dist": np.zeros(n, np.float32),
                "normal": np.zeros((n, 3), np.float32), "status": np.zeros(n, np.int32)}
     P = ctypes.c_void_p
-    check(ctx.lib.ogx_gjk_epa_streamed(ctx.handle, pool.handle, P(ptr(coords)), n, P(ptr(pairs)),
-                                       P(ptr(out["simplex"])), P(ptr(out["dist"])), P(ptr(out["normal"])),
-                                       P(ptr(out["status"])), int(chunks)))
+    args = (ctx.handle, pool.handle, P(ptr(coords)), n, P(ptr(pairs)), P(ptr(out["simplex"])),
+            P(ptr(out["dist"])), P(ptr(out["normal"])), P(ptr(out["status"])))
+    if bounds is None:
+        check(ctx.lib.ogx_gjk_epa_streamed(*args, int(chunks)))
+    else:
+        b = np.ascontiguousarray(bounds, dtype=np.int32)
+        check(ctx.lib.ogx_gjk_epa_streamed_ranges(*args, P(b.ctypes.data), int(b.shape[0]) - 1, int(lanes)))
     return out
 
 

@@ -188,3 +188,34 @@ def test_streamed_call_matches_batched(engine, chunks):
     assert np.array_equal(out["dist"], ref["dist"])
     assert np.array_equal(out["normal"], ref["normal"])
     assert np.array_equal(out["simplex"]["witnesses"], ref["simplex"]["witnesses"])
+
+
+@pytest.mark.parametrize("lanes", [1, 3, 8])
+def test_streamed_ranges_match_batched(engine, lanes):
+    """Caller-given pair ranges (uneven, some empty, bad indices inside) and lane counts
+    give the results of the device call; bad range bounds are refused."""
+    import torch
+    from ogx import _lib
+    b = W.powerlaw(seed=45, n_pairs=3000)
+    pairs = np.ascontiguousarray(b.pairs.copy())
+    pairs[50] = (0, 10 ** 7)                     # flagged, needs no body
+    pairs[2990] = (3, 1)                         # last range refers to early bodies
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    coords = torch.from_numpy(b.coords).pin_memory()
+    bounds = [0, 10, 10, 700, 701, 2500, 2999, 3000]
+    out = engine.streamed(ctx, pool, coords, pairs, bounds=bounds, lanes=lanes)
+    ref = engine.run(ctx, pool, torch.from_numpy(pairs).cuda()).to_host()
+    ctx.synchronize()
+    assert out["status"][50] & _lib.PAIR_BAD_INPUT
+    ok = np.ones(len(pairs), bool)
+    ok[50] = False
+    assert np.array_equal(out["dist"][ok], ref["dist"][ok])
+    assert np.array_equal(out["normal"], ref["normal"], equal_nan=True)
+    assert np.array_equal(out["simplex"]["witnesses"][ok], ref["simplex"]["witnesses"][ok])
+    assert np.array_equal(out["status"], ref["status"])
+    for bad in ([0, 5, 3, 3000], [1, 3000], [0, 2999], [0]):
+        with pytest.raises(RuntimeError):
+            engine.streamed(ctx, pool, coords, pairs, bounds=bad, lanes=lanes)
+    with pytest.raises(RuntimeError):
+        engine.streamed(ctx, pool, coords, pairs, bounds=[0, 3000], lanes=9)
