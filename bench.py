@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--choice", default="",
                     help='kernel variants instead of autotuning, as printed in "kernel_choice" (JSON)')
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip timing the reference's own GPU kernels on the same workload")
     ap.add_argument("--chunks", type=int, default=8, help="pieces of the end-to-end streamed call")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
@@ -152,6 +154,68 @@ def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
     return {"value": n / dt, "unit": "pairs/s", "cores": threads if not use_ref else threads,
             "kind": kind, "sample": f"first {n} pairs of the workload, FP32 reference tolerances, "
                                    f"{threads} threads, {dt:.1f} s"}
+
+
+def plain_form_baseline(batch, device: int, steps: int = 3) -> dict:
+    """The reference's own GPU kernels (GJK/gpu/openGJK.cu, FP32 as shipped, compiled for
+    sm_103a) on the same workload with the points resident: its fused indexed call's
+    device part (simplices zeroed, GJK kernel, EPA kernel) per step, CUDA events."""
+    import torch
+    from oracle import plain_form
+    if not plain_form.available():
+        return {"unavailable": "the reference's GPU kernels were not compiled (needs the reference sources)"}
+    dev = torch.device("cuda", device)
+    coords = torch.from_numpy(batch.coords).to(dev)
+    pairs = torch.from_numpy(np.ascontiguousarray(batch.pairs)).to(dev)
+    pf = plain_form.PlainForm(device).load(coords, batch.offsets, batch.counts)
+    st = torch.cuda.Stream(dev)
+    with torch.cuda.stream(st):
+        out = pf.run(pairs)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(st)
+    with torch.cuda.stream(st):
+        for _ in range(steps):
+            pf.run(pairs, out)
+    ev1.record(st)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / steps
+    # host to host as the reference's fused indexed call moves the data
+    # (GJK/gpu/openGJK.cu:3274-3310; its allocations and frees left out): points and body
+    # descriptors up from pinned memory, pairs up, kernels, simplices / distances / normals
+    # down to pinned memory
+    h_coords = torch.from_numpy(batch.coords).pin_memory()
+    h_desc = pf.polytopes.cpu().pin_memory()
+    h_pairs = torch.from_numpy(np.ascontiguousarray(batch.pairs)).pin_memory()
+    h_out = {k: torch.empty(v.shape, dtype=v.dtype).pin_memory() for k, v in out.items()}
+    h2d = h_coords.numel() * 4 + h_desc.numel() + h_pairs.numel() * 4
+    d2h = sum(t.numel() * t.element_size() for t in h_out.values())
+
+    def host_step():
+        with torch.cuda.stream(st):
+            coords.copy_(h_coords, non_blocking=True)
+            pf.polytopes.copy_(h_desc, non_blocking=True)
+            pairs.copy_(h_pairs, non_blocking=True)
+            pf.run(pairs, out)
+            for k in h_out:
+                h_out[k].copy_(out[k], non_blocking=True)
+        st.synchronize()
+    host_step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        host_step()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
+    pf.close()
+    return {"value": batch.n_pairs / (ms / 1e3), "unit": "pairs/s", "ms_per_step": ms, "steps": steps,
+            "e2e": {"value": batch.n_pairs / (e2e_ms / 1e3), "unit": "pairs/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "path": "the reference's indexed call sequence without its allocations: copies up, "
+                            "kernels, copies down, in order on one stream, host clock"},
+            "kind": "reference GPU kernels",
+            "source": "GJK/gpu/openGJK.cu indexed GJK + EPA kernels, FP32 as shipped, compiled for sm_103a, "
+                      "shipped launch shapes (GJK: 256-thread blocks, 8 threads per pair; EPA: 4 pairs of "
+                      "32 threads per block, 39,264 B shared memory)",
+            "sample": "the whole workload, points resident in HBM, 1 warm-up step"}
 
 
 def serving_report(device: int, seed: int = 77) -> dict:
@@ -517,6 +581,12 @@ def run_ours(args):
         line["e2e"] = e2e
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(batch)
+    if not args.no_plain and world == 1:
+        line["plain_form"] = plain_form_baseline(batch, local)
+        if "value" in line["plain_form"]:
+            line["plain_form"]["engine_speedup"] = value / line["plain_form"]["value"]
+            if e2e:
+                line["plain_form"]["engine_e2e_speedup"] = e2e["value"] / line["plain_form"]["e2e"]["value"]
     if not args.no_serving:
         graph.close()
         del out, pairs
