@@ -79,6 +79,8 @@ typedef struct ogx_config {
 #define OGX_PAIR_EPA_TOPOLOGY 256
 #define OGX_PAIR_EPA_CAPACITY 512
 #define OGX_PAIR_EPA_ESCALATED 1024
+#define OGX_PAIR_EPA_CERTIFIED 2048 /* the expansion ran again with FP64 planes and exact
+                                     * supports until the FP64 test converged */
 #define OGX_PAIR_BAD_INPUT 16384
 
 ogx_status ogx_config_default(ogx_config* cfg);

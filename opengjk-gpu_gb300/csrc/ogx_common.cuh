@@ -26,9 +26,12 @@
 #endif
 
 #if !defined(__CUDACC__)
-// the two CUDA vector types the algorithm uses, for the host build
+// the CUDA vector types the algorithm uses, for the host build
 struct float4 {
   float x, y, z, w;
+};
+struct double4 {
+  double x, y, z, w;
 };
 struct int2 {
   int x, y;
@@ -39,6 +42,14 @@ namespace ogx {
 
 OGX_HD float4 make_float4_(float x, float y, float z, float w) {
   float4 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  r.w = w;
+  return r;
+}
+OGX_HD double4 make_double4_(double x, double y, double z, double w) {
+  double4 r;
   r.x = x;
   r.y = y;
   r.z = z;
@@ -144,6 +155,7 @@ enum {
   OGX_S_EPA_TOPOLOGY = OGX_PAIR_EPA_TOPOLOGY,
   OGX_S_EPA_CAPACITY = OGX_PAIR_EPA_CAPACITY,
   OGX_S_EPA_ESCALATED = OGX_PAIR_EPA_ESCALATED,
+  OGX_S_EPA_CERTIFIED = OGX_PAIR_EPA_CERTIFIED,
   OGX_S_BAD_INPUT = OGX_PAIR_BAD_INPUT,
 };
 

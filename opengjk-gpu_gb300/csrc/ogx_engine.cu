@@ -689,17 +689,29 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     }
     if (e == cudaSuccess) e = join_in();
     if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA launches");
-    // contacts that outgrew the bucket kernels' working set, at full capacity
+    // contacts that outgrew the bucket kernels' working set or need the certified re-run,
+    // at full capacity (polished in the same kernel), beside the polish of the others
     ctx->mark("epa_spill");
-    e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), st);
+    cudaStream_t sst = st;
+    if (fork) {
+      e = cudaEventRecord(ctx->fork_ev, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
+      sst = ctx->aux[0];
+    }
+    if (e == cudaSuccess) e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), sst);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
     ++launches;
-  }
-  if (mode != kModeGjk && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
-    ctx->mark("polish");
-    e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), st);
-    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
-    ++launches;
+    if (ctx->cfg.flags & OGX_F_FP64_POLISH) {
+      ctx->mark("polish");
+      e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), st);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
+      ++launches;
+    }
+    if (fork) {
+      e = cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->join_ev[0], 0);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "spill join");
+    }
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return ogx_cuda_fail(e, "pipeline launch");

@@ -51,6 +51,23 @@ typedef EpaMemT<kEpaVmax, kEpaFmax> EpaMem;
 // small capacity: 24 expansions; a pair that needs more is handed to a full-capacity pass
 constexpr int kEpaSmallIters = 24;
 typedef EpaMemT<4 + kEpaSmallIters, 4 + 2 * kEpaSmallIters> EpaMemSmall;
+// full capacity for the certified re-run: every face's plane is also kept in FP64
+struct EpaMemCert : EpaMem {
+  double4 fn64[kEpaFmax];  // unit outward normal and plane distance, FP64 from exact points
+};
+OGX_HD double4* plane64_slot(EpaMemCert& M, int f) { return &M.fn64[f]; }
+template <class Mem>
+OGX_HD double4* plane64_slot(Mem&, int) { return nullptr; }
+
+// The certified re-run.  An FP32 expansion that stops with the support still above the
+// closest face by more than rounding (kEpaCertGain * scale; the FP32 test accepts up to
+// epa_rel * scale), or whose support repeats a vertex before converging, is run again at
+// full capacity with every face plane in FP64 from the exact points, visibility decided
+// on those planes, exact (FP64) supports, and convergence when the support improves on
+// the closest face by at most kEpaCertTol * max(1, scale).
+constexpr float kEpaCertGain = 2.5e-7f;
+constexpr double kEpaCertTol = 1e-10;
+constexpr double kEpaCertVis = 1e-12;
 
 struct EpaOut {
   float dist;   // -depth for contacts, the GJK distance otherwise
@@ -85,7 +102,7 @@ OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
 template <class Mem, class Bodies>
 OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, bool escalate, bool all64,
-                         int& status) {
+                         int& status, double4* p64 = nullptr) {
   const float4 P0 = M.vp[a], P1 = M.vp[b], P2 = M.vp[c];
   const fv3 p0 = v3<float>(P0.x, P0.y, P0.z);
   const fv3 e0 = v3<float>(P1.x, P1.y, P1.z) - p0;
@@ -108,9 +125,11 @@ OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, boo
       r.y = (float)(m.y * inv);
       r.z = (float)(m.z * inv);
       r.w = (float)(dot(m, q0) * inv);
+      if (p64) *p64 = make_double4_(m.x * inv, m.y * inv, m.z * inv, dot(m, q0) * inv);
     } else {
       r.x = r.y = r.z = 0.0f;
       r.w = INFINITY;  // degenerate: never the closest face, never visible
+      if (p64) *p64 = make_double4_(0.0, 0.0, 0.0, (double)INFINITY);
     }
     return r;
   }
@@ -285,13 +304,16 @@ OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
 //   4. new faces are linked to each other through the per-vertex tables and their planes
 //      computed; the closest new face joins the lane's candidate.
 // The next step's closest face is the team's minimum over the candidates.
-template <class Team, class Bodies, class Mem>
+// kCert (the full-capacity re-run only): with FP64 face planes on, run the certified
+// expansion described at kEpaCertGain.
+template <bool kCert = false, class Team, class Bodies, class Mem>
 OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const GjkState& g,
                      Mem& M, EpaOut& o, bool can_spill) {
   const int L = Team::L;
   const int lane = t.lane();
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
   const bool all64 = (cfg.flags & OGX_F_EPA_FP64_PLANES) != 0;
+  const bool cert = kCert && all64;
   o.status = 0;
   o.iters = 0;
   o.polish = false;
@@ -406,7 +428,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     M.fa[f][0] = (uint8_t)(f == 0 ? 3 : 0);
     M.fa[f][1] = (uint8_t)(f == 0 || f == 1 ? 2 : (f == 2 ? 3 : 1));
     M.fa[f][2] = (uint8_t)(f == 0 ? 1 : (f == 1 ? 3 : (f == 2 ? 1 : 2)));
-    const float4 pl = face_plane(M, B, va, vb, vc, escalate, all64, st);
+    const float4 pl = face_plane(M, B, va, vb, vc, escalate, all64, st, plane64_slot(M, f));
     M.fn[f] = pl;
     if (pl.w < cbd) {
       cbd = pl.w;
@@ -435,11 +457,35 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     const float4 nf = M.fn[best];
     const fv3 n = v3<float>(nf.x, nf.y, nf.z);
     int qa, qb;
-    const fv3 q = msupport(t, B, n, qa, qb);
-    const float scale = sqrtf(fmaxf(scale2, dot(q, q)));
-    const float tol = fmaxf(tol_floor, cfg.epa_rel * scale);
-    const float gain = dot(n, q) - bd;
-    if (gain < tol) {
+    fv3 q;
+    dv3 q64 = v3<double>(0.0, 0.0, 0.0);
+    float scale;
+    bool conv;
+    float gain = 0.0f;
+    if (cert) {
+      // exact supports along the closest face's FP64 normal
+      const double4 pl = *plane64_slot(M, best);
+      const dv3 n64 = v3<double>(pl.x, pl.y, pl.z);
+      double ha, hb;
+      qa = exact_support(t, B, 0, n64, ha);
+      qb = exact_support(t, B, 1, -n64, hb);
+      q = B.point(0, qa) - B.point(1, qb);
+      q64 = B.dpoint(0, qa) - B.dpoint(1, qb);
+      scale = sqrtf(fmaxf(scale2, dot(q, q)));
+      conv = !(ha + hb - pl.w > kEpaCertTol * fmax(1.0, (double)scale));
+    } else {
+      q = msupport(t, B, n, qa, qb);
+      scale = sqrtf(fmaxf(scale2, dot(q, q)));
+      const float tol = fmaxf(tol_floor, cfg.epa_rel * scale);
+      gain = dot(n, q) - bd;
+      conv = gain < tol;
+    }
+    if (conv) {
+      if (!cert && escalate && can_spill && !all64 && gain > kEpaCertGain * scale) {
+        o.spill = true;
+        o.spill64 = true;
+        return;
+      }
       o.status |= OGX_S_EPA_CONVERGED;
       done = true;
       break;
@@ -450,6 +496,13 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       dup |= (id.x == qa && id.y == qb);
     }
     if (t.any(dup)) {
+      // the support is already a vertex although the closest face is not converged:
+      // FP32 planes put a vertex in front of a face; re-run certified
+      if (!cert && escalate && can_spill && !all64) {
+        o.spill = true;
+        o.spill64 = true;
+        return;
+      }
       o.status |= OGX_S_EPA_DUPLICATE;
       done = true;
       break;
@@ -481,7 +534,12 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       bool s = false;
       if (f < fend && M.fv[f][3]) {
         const float4 fp = M.fn[f];
-        s = (fp.x * q.x + fp.y * q.y + fp.z * q.z) - fp.w > vis_eps;
+        if (cert) {
+          const double4 pl = *plane64_slot(M, f);
+          s = (pl.x * q64.x + pl.y * q64.y + pl.z * q64.z) - pl.w > kEpaCertVis * (double)scale;
+        } else {
+          s = (fp.x * q.x + fp.y * q.y + fp.z * q.z) - fp.w > vis_eps;
+        }
         if (!s && fp.w < cbd) {
           cbd = fp.w;
           cbest = f;
@@ -589,7 +647,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       M.fa[s][0] = M.hz[k][2];
       M.fa[s][1] = M.hstart[b];
       M.fa[s][2] = M.hend[a];
-      const float4 pl = face_plane(M, B, a, b, p, escalate, all64, st);
+      const float4 pl = face_plane(M, B, a, b, p, escalate, all64, st, plane64_slot(M, s));
       M.fn[s] = pl;
       M.fv[s][3] = 1;
       if (pl.w < cbd || (pl.w == cbd && s < cbest)) {
@@ -602,6 +660,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   }
   o.iters = it;
   o.status |= st ? OGX_S_EPA_ESCALATED : 0;
+  o.status |= cert ? OGX_S_EPA_CERTIFIED : 0;
   if (!done) {
     // iteration cap: closest current face
     float bd = cbd;

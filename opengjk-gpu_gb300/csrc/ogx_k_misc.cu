@@ -260,14 +260,15 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// EPA at full capacity (EpaMem) over the spill list, every face plane from FP64 for the
-// contacts whose FP32 expansion met an inconsistent horizon: one warp per contact,
-// points read from memory (any body size)
+// EPA at full capacity over the spill list: contacts that ran out of the small working
+// set, and -- certified, every face plane from FP64, exact supports -- contacts whose FP32
+// expansion met an inconsistent horizon or stopped short of the FP32 rounding level.
+// One warp per contact, points read from memory (any body size).
 __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  EpaMem* mem = reinterpret_cast<EpaMem*>(smem_raw);
+  EpaMemCert* mem = reinterpret_cast<EpaMemCert*>(smem_raw);
   const WarpTeam<32> t;
-  EpaMem& M = mem[threadIdx.x / 32];
+  EpaMemCert& M = mem[threadIdx.x / 32];
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int nteams = (gridDim.x * blockDim.x) / 32;
   const int cnt = B.counts[kCntSpill];
@@ -275,19 +276,19 @@ __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
   cfg64.flags |= OGX_F_EPA_FP64_PLANES;
   for (int j = team; j < cnt; j += nteams) {
     const int e = B.spill[j];
-    epa_item<32, 0>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
+    epa_item<32, 0, true>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
     t.sync();
   }
 }
 
 cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st) {
-  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMem), st>>>(B);
+  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B);
   return cudaGetLastError();
 }
 
 cudaError_t epa_spill_occupancy(int block, int* per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_epa_spill, block,
-                                                       (block / 32) * sizeof(EpaMem));
+                                                       (block / 32) * sizeof(EpaMemCert));
 }
 
 cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {

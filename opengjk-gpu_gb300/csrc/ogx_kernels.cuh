@@ -210,7 +210,10 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
 // spill list entries: pair index, top bit set when the re-run needs FP64 face planes
 constexpr int kSpill64 = 1 << 30;
 
-template <int L, int K, class Mem>
+// kFull: the full-capacity pass over the spill list -- certified re-runs where the entry
+// asks for FP64 planes, and the FP64 polish of the result done here by lane 0 instead of
+// through the polish list, so that the polish pass need not wait for this one
+template <int L, int K, bool kFull = false, class Mem>
 __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
                                          Mem& M, bool can_spill, bool* spill64 = nullptr) {
   const int2 pr = B.pairs[p];
@@ -219,12 +222,16 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
   GjkState g;
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
-  epa_pair(t, src, cfg, g, M, o, can_spill);
+  epa_pair<kFull>(t, src, cfg, g, M, o, can_spill);
   if (o.spill) {
     if (spill64) *spill64 = o.spill64;
     return false;
   }
   const bool lead = t.lane() == 0;
+  if (kFull && lead && o.polish) {
+    epa_polish(src, o);
+    o.polish = false;
+  }
   if (lead) {
     B.dist[p] = o.dist;
     gkSimplex* s = B.smp + p;

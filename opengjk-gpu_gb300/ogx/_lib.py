@@ -37,6 +37,7 @@ PAIR_EPA_TOUCH = 128
 PAIR_EPA_TOPOLOGY = 256
 PAIR_EPA_CAPACITY = 512
 PAIR_EPA_ESCALATED = 1024
+PAIR_EPA_CERTIFIED = 2048
 PAIR_BAD_INPUT = 16384
 
 # gkSimplex, FP32 layout of the reference (GJK/common.h:84-89): 108 bytes

@@ -32,7 +32,7 @@ struct Job {
 
 struct Work {
   EpaMemSmall small;
-  EpaMem full;
+  EpaMemCert full;
 };
 
 void one(const Job& J, int i, Work& M) {
@@ -71,7 +71,7 @@ void one(const Job& J, int i, Work& M) {
       if (o.spill) {
         ogx_config c = *J.cfg;
         if (o.spill64) c.flags |= OGX_F_EPA_FP64_PLANES;
-        epa_pair(t, B, c, g, M.full, o, false);
+        epa_pair<true>(t, B, c, g, M.full, o, false);
       }
       if (o.polish) epa_polish(B, o);
       d = o.dist;
