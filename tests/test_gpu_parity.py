@@ -142,9 +142,9 @@ def test_stress_200k_error_report(engine, orc):
     """Mixed-precision stress set at its full size (200k pairs): error of every output
     against the FP64 oracle, per kind.  Verdicts and distances meet the parity rules for
     every kind, depths, normals and witnesses for all but the 1e-4-thick disks, where the
-    minimum translation direction is barely resolved by FP32 inputs: there at most one
-    depth in 10^4 may miss and 99% of the normals are within 1e-4 (the report gives the
-    rest, and how far the depth along each other normal is from the oracle's)."""
+    minimum translation direction is barely resolved by FP32 inputs: there every depth
+    meets the rule and 99.9% of the normals are within 1e-4 (the report gives the rest,
+    and how far the depth along each other normal is from the oracle's)."""
     import json
     b = W.stress(seed=9, n_pairs=200_000)
     res = engine.query(b, engine.MODE_GJK_EPA)
@@ -157,8 +157,9 @@ def test_stress_200k_error_report(engine, orc):
         if name != "thin_disks":
             parity.assert_parity(r, max_witness_mismatch_frac=2e-3)
         else:
-            # 1e-4-thick near-coplanar disks: the FP32 expansion can meet an inconsistent
-            # horizon; such contacts run again with FP64 planes, and the few that still
-            # stop early are counted here
-            assert r["depth_violations"] <= max(1, 1e-4 * r["contacts"]), r
-            assert r["normal_within_1e-4_frac"] > 0.99, r
+            # 1e-4-thick near-coplanar disks: contacts whose FP32 expansion meets an
+            # inconsistent horizon or stops above rounding run again certified; a few
+            # whose FP32 face normal is off by ~1e-6 (enough to pick another support
+            # without the FP32 gain showing it) keep a normal within ~4e-4
+            assert r["depth_violations"] == 0, r
+            assert r["normal_within_1e-4_frac"] >= 0.999, r
