@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the kernel autotuner")
+    ap.add_argument("--tune-reps", type=int, default=3, help="timed runs per candidate in the autotuner (best kept)")
     ap.add_argument("--choice", default="",
                     help='kernel variants instead of autotuning, as printed in "kernel_choice" (JSON)')
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
@@ -428,7 +429,7 @@ def run_ours(args):
                 ctx.set_kernel_choice(kind, b, L, K)
         choice = ctx.kernel_choice()
     else:
-        choice = ctx.autotune(pool, pairs, reps=1) if not args.no_tune else ctx.kernel_choice()
+        choice = ctx.autotune(pool, pairs, reps=args.tune_reps) if not args.no_tune else ctx.kernel_choice()
     torch.cuda.synchronize()
 
     # one instrumented step: per-kernel CUDA-event times and work counts
