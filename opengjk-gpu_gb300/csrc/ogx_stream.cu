@@ -14,7 +14,6 @@
 
 #include <algorithm>
 #include <cstdlib>
-#include <thread>
 #include <vector>
 
 #include "ogx_engine.h"
@@ -112,23 +111,6 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
   if (!s) s = ctx->ensure_stage(0, (size_t)pool->npoints * 3 * sizeof(float));
   if (s) return s;
 
-  // the highest body each pair range references (host threads)
-  std::vector<int> need(C, -1);
-  {
-    std::vector<std::thread> th;
-    for (int j = 0; j < C; ++j)
-      th.emplace_back([&, j] {
-        int m = -1;
-        for (int i = pb[j]; i < pb[j + 1]; ++i) m = std::max(m, std::max(pairs[i].idx1, pairs[i].idx2));
-        need[j] = m;
-      });
-    for (auto& t : th) t.join();
-  }
-  // body range k holds the bodies that pair range k references first: chunk k then waits
-  // only for body ranges 0..k (indices out of range need no body; the kernels flag them)
-  std::vector<int> bb(C + 1, nb);
-  bb[0] = 0;
-  for (int k = 0; k + 1 < C; ++k) bb[k + 1] = std::max(bb[k], std::min(nb, need[k] + 1));
   // optional timeline (context timing on): per chunk, the end of its body upload, the end
   // of its pair upload, its compute start and end, the end of its download
   const bool tl = ctx->timing;
@@ -149,12 +131,21 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
   cudaEvent_t* ev_packed = ev_done + C;
   const float* d_aos = static_cast<const float*>(ctx->d_stage);
   cudaError_t e = cudaSuccess;
-  // uploads, interleaved so that pair range j follows the bodies it most likely needs
+  // Body range k holds the bodies that pair range k references first: chunk k then waits
+  // only for body ranges 0..k (indices out of range need no body; the kernels flag them).
+  // Each range is cut, uploaded and launched before the next one's pairs are scanned, so
+  // that the scan of later ranges overlaps the copies already in flight.
+  std::vector<int> bb(C + 1, nb);
+  bb[0] = 0;
+  int launches = 0;
+  int need = -1;  // highest body referenced by pair ranges 0..k
   for (int k = 0; k < C && e == cudaSuccess; ++k) {
-    const int64_t p0 = bb[k] < nb ? pool->h_voff[bb[k]] : pool->npoints;
-    const int64_t p1 = bb[k + 1] < nb ? pool->h_voff[bb[k + 1]] : pool->npoints;
-    if (p1 > p0)
-      e = cudaMemcpyAsync(const_cast<float*>(d_aos) + 3 * p0, xyz + 3 * p0, (p1 - p0) * 3 * sizeof(float),
+    for (int i = pb[k]; i < pb[k + 1]; ++i) need = std::max(need, std::max(pairs[i].idx1, pairs[i].idx2));
+    if (k + 1 < C) bb[k + 1] = std::max(bb[k], std::min(nb, need + 1));
+    const int64_t v0 = bb[k] < nb ? pool->h_voff[bb[k]] : pool->npoints;
+    const int64_t v1 = bb[k + 1] < nb ? pool->h_voff[bb[k + 1]] : pool->npoints;
+    if (v1 > v0)
+      e = cudaMemcpyAsync(const_cast<float*>(d_aos) + 3 * v0, xyz + 3 * v0, (v1 - v0) * 3 * sizeof(float),
                           cudaMemcpyHostToDevice, ctx->up);
     if (e == cudaSuccess) e = cudaEventRecord(ev_body[k], ctx->up);
     mark(k, 0, ctx->up);
@@ -163,12 +154,10 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
                           cudaMemcpyHostToDevice, ctx->up);
     if (e == cudaSuccess) e = cudaEventRecord(ev_pair[k], ctx->up);
     mark(k, 1, ctx->up);
-  }
-  if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed upload");
-  // chunk j of the pairs runs on lane j % S once the bodies it needs are packed and its
-  // pairs are up
-  int launches = 0;
-  for (int j = 0; j < C; ++j) {
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed upload");
+    // chunk k of the pairs runs on lane k % S once the bodies it needs are packed and its
+    // pairs are up
+    const int j = k;
     // body range j, packed in order on the context's stream: ranges 0..j then hold every
     // body that pair range j references
     e = cudaStreamWaitEvent(ctx->stream, ev_body[j], 0);
