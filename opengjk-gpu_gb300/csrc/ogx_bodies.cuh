@@ -65,7 +65,37 @@ struct MemBodies {
     const float* X = base[w];
     const float* Y = X + n4[w];
     const float* Z = X + 2 * n4[w];
-    for (int q = t.lane(); q < nb; q += Team::L) {
+    int q = t.lane();
+#if defined(__CUDA_ARCH__)
+    // two blocks per step, both blocks' loads issued before either is compared (twice the
+    // loads in flight); blocks are still compared in increasing index order
+    const float4* X4 = reinterpret_cast<const float4*>(X);
+    const float4* Y4 = reinterpret_cast<const float4*>(Y);
+    const float4* Z4 = reinterpret_cast<const float4*>(Z);
+    for (; q + Team::L < nb; q += 2 * Team::L) {
+      const int q2 = q + Team::L;
+      const float4 x = __ldg(X4 + q), y = __ldg(Y4 + q), z = __ldg(Z4 + q);
+      const float4 x2 = __ldg(X4 + q2), y2 = __ldg(Y4 + q2), z2 = __ldg(Z4 + q2);
+      float v;
+      v = sdot(x.x, y.x, z.x, d);
+      if (v > best) { best = v; bi = 4 * q; }
+      v = sdot(x.y, y.y, z.y, d);
+      if (v > best) { best = v; bi = 4 * q + 1; }
+      v = sdot(x.z, y.z, z.z, d);
+      if (v > best) { best = v; bi = 4 * q + 2; }
+      v = sdot(x.w, y.w, z.w, d);
+      if (v > best) { best = v; bi = 4 * q + 3; }
+      v = sdot(x2.x, y2.x, z2.x, d);
+      if (v > best) { best = v; bi = 4 * q2; }
+      v = sdot(x2.y, y2.y, z2.y, d);
+      if (v > best) { best = v; bi = 4 * q2 + 1; }
+      v = sdot(x2.z, y2.z, z2.z, d);
+      if (v > best) { best = v; bi = 4 * q2 + 2; }
+      v = sdot(x2.w, y2.w, z2.w, d);
+      if (v > best) { best = v; bi = 4 * q2 + 3; }
+    }
+#endif
+    for (; q < nb; q += Team::L) {
 #if defined(__CUDA_ARCH__)
       const float4 x = __ldg(reinterpret_cast<const float4*>(X) + q);
       const float4 y = __ldg(reinterpret_cast<const float4*>(Y) + q);
