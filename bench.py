@@ -485,9 +485,12 @@ def run_ours(args):
 
         e2e_step()
         torch.cuda.synchronize()
+        per_call = []
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            t1 = time.perf_counter()
             e2e_step()
+            per_call.append((time.perf_counter() - t1) * 1e3)
         ems = (time.perf_counter() - t0) * 1e3 / e2e_steps
         if world > 1:
             t = torch.tensor([ems], device="cuda")
@@ -513,6 +516,9 @@ def run_ours(args):
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "path": f"ogx_gjk_epa_streamed (pool points and pairs up, results down, {args.chunks} chunks "
                        "overlapped with the kernels), pinned host buffers, host clock",
+               "calls": e2e_steps,
+               "call_ms": {"min": round(min(per_call), 3), "median": round(statistics.median(per_call), 3),
+                           "max": round(max(per_call), 3)},
                "serial_phases_ms": serial}
 
     if rank != 0:

@@ -149,7 +149,8 @@ int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
  * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16],
  * contacts whose EPA outgrew the bucket kernels' working set and ran again at full
  * capacity [17], FP64 continuations of pairs with a body above 128 points (one warp
- * each; the others in [16] - [18] run one thread each) [18].  cap must be >= 19. */
+ * each; the others in [16] - [18] run one thread each) [18], contacts that only the
+ * FP64 refinement found (certified full-capacity EPA) [19].  cap must be >= 20. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 /* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most

@@ -315,6 +315,12 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
     if (ctx->join_ev[b]) cudaEventDestroy(ctx->join_ev[b]);
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->aux_r) {
+    cudaStreamSynchronize(ctx->aux_r);
+    cudaStreamDestroy(ctx->aux_r);
+  }
+  if (ctx->route_ev) cudaEventDestroy(ctx->route_ev);
+  if (ctx->rjoin_ev) cudaEventDestroy(ctx->rjoin_ev);
   cudaFree(ctx->d_io_pairs);
   cudaFree(ctx->d_io_smp);
   cudaFree(ctx->d_io_dist);
@@ -424,12 +430,15 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
 ogx_status ogx_ctx::ensure_aux() {
   if (fork_ev) return OGX_OK;
   cudaError_t e;
-  for (int b = 0; b < kBuckets; ++b) {
+  for (int b = 0; b < fork_width; ++b) {
     if ((e = cudaStreamCreateWithFlags(&aux[b], cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&join_ev[b], cudaEventDisableTiming)) != cudaSuccess)
       return ogx_cuda_fail(e, "bucket streams");
   }
-  if ((e = cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming)) != cudaSuccess)
+  if ((e = cudaStreamCreateWithFlags(&aux_r, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&route_ev, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&rjoin_ev, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming)) != cudaSuccess)
     return ogx_cuda_fail(e, "bucket streams");
   return OGX_OK;
 }
@@ -641,17 +650,18 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   // and joined back into the context's stream) so that the tail of one bucket overlaps
   // the others' work; with per-kernel timing on they run in sequence.
   const bool fork = !ctx->timing && ctx->fork_ok && ctx->ensure_aux() == OGX_OK;
-  auto bucket_stream = [&](int b) -> cudaStream_t { return fork ? ctx->aux[b] : st; };
+  const int W = ctx->fork_width;  // bucket b runs on aux[b mod W]
+  auto bucket_stream = [&](int b) -> cudaStream_t { return fork ? ctx->aux[b % W] : st; };
   auto fork_out = [&]() -> cudaError_t {
     if (!fork) return cudaSuccess;
     cudaError_t r = cudaEventRecord(ctx->fork_ev, st);
-    for (int b = 0; b < kBuckets && r == cudaSuccess; ++b) r = cudaStreamWaitEvent(ctx->aux[b], ctx->fork_ev, 0);
+    for (int b = 0; b < W && r == cudaSuccess; ++b) r = cudaStreamWaitEvent(ctx->aux[b], ctx->fork_ev, 0);
     return r;
   };
   auto join_in = [&]() -> cudaError_t {
     if (!fork) return cudaSuccess;
     cudaError_t r = cudaSuccess;
-    for (int b = 0; b < kBuckets && r == cudaSuccess; ++b) {
+    for (int b = 0; b < W && r == cudaSuccess; ++b) {
       r = cudaEventRecord(ctx->join_ev[b], ctx->aux[b]);
       if (r == cudaSuccess) r = cudaStreamWaitEvent(st, ctx->join_ev[b], 0);
     }
@@ -668,17 +678,12 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     if (e == cudaSuccess) e = join_in();
     if (e != cudaSuccess) return ogx_cuda_fail(e, "GJK launches");
   }
-  if (mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH)) {
-    ctx->mark("refine");
-    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st,
-                      fork ? ctx->aux[0] : st, fork ? ctx->fork_ev : nullptr);
-    if (e == cudaSuccess && fork) {
-      e = cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->join_ev[0], 0);
-    }
-    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
-    launches += 3;
-  }
+  // The FP64 refinement (separated pairs) and the EPA buckets (contacts) touch disjoint
+  // pairs: forked, the refinement runs on the context's stream (and aux_r) beside the EPA
+  // buckets, followed there by the full-capacity pass over the few contacts it finds; the
+  // spill and polish passes of the buckets' contacts wait for the buckets only, and
+  // everything joins back into the context's stream.
+  const bool refine = mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH);
   if (mode != kModeGjk) {
     e = fork_out();
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
@@ -687,29 +692,55 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
       k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
       ++launches;
     }
-    if (e == cudaSuccess) e = join_in();
     if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA launches");
+  }
+  if (refine) {
+    ctx->mark("refine");
+    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st,
+                      fork ? ctx->aux_r : st, fork ? ctx->route_ev : nullptr);
+    if (e == cudaSuccess && fork) {
+      e = cudaEventRecord(ctx->rjoin_ev, ctx->aux_r);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->rjoin_ev, 0);
+    }
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
+    launches += 3;
+    if (mode != kModeGjk) {
+      // the contacts the refinement found (usually none), after it on the same stream
+      ctx->mark("epa_late");
+      e = launch_epa_spill(B, fit_grid(g_grid_spill, std::max(1, npairs / 256), 32), st, true);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
+      ++launches;
+    }
+  }
+  if (mode != kModeGjk) {
     // contacts that outgrew the bucket kernels' working set or need the certified re-run,
     // at full capacity (polished in the same kernel), beside the polish of the others
-    ctx->mark("epa_spill");
-    cudaStream_t sst = st;
+    cudaStream_t sst = st, pst = st;
     if (fork) {
-      e = cudaEventRecord(ctx->fork_ev, st);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
       sst = ctx->aux[0];
+      pst = ctx->aux[1];
+      for (int b = 0; b < W && e == cudaSuccess; ++b) e = cudaEventRecord(ctx->join_ev[b], ctx->aux[b]);
+      for (int b = 0; b < W && e == cudaSuccess; ++b) {
+        if (b != 0) e = cudaStreamWaitEvent(sst, ctx->join_ev[b], 0);
+        if (e == cudaSuccess && b != 1) e = cudaStreamWaitEvent(pst, ctx->join_ev[b], 0);
+      }
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA join");
     }
-    if (e == cudaSuccess) e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), sst);
+    ctx->mark("epa_spill");
+    e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), sst);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
     ++launches;
     if (ctx->cfg.flags & OGX_F_FP64_POLISH) {
       ctx->mark("polish");
-      e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), st);
+      e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), pst);
       if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
       ++launches;
     }
     if (fork) {
-      e = cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
+      e = cudaEventRecord(ctx->join_ev[0], sst);
+      if (e == cudaSuccess) e = cudaEventRecord(ctx->join_ev[1], pst);
       if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->join_ev[0], 0);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->join_ev[1], 0);
       if (e != cudaSuccess) return ogx_cuda_fail(e, "spill join");
     }
   }

@@ -41,9 +41,12 @@ struct ogx_ctx {
   void mark(const char* name);  // record an event before the next launch
   // concurrent bucket launches: one stream per size bucket, fork / join events
   bool fork_ok = true;
+  int fork_width = ogx::kBuckets;  // bucket streams when forked (2..kBuckets; fixed once created)
   cudaStream_t aux[ogx::kBuckets] = {};
   cudaEvent_t fork_ev = nullptr;
   cudaEvent_t join_ev[ogx::kBuckets] = {};
+  cudaStream_t aux_r = nullptr;  // the FP64 refinement's second kernel, beside the EPA buckets
+  cudaEvent_t route_ev = nullptr, rjoin_ev = nullptr;
   ogx_status ensure_aux();
   // streamed host-to-host calls: copy streams, events, device input/output buffers
   cudaStream_t up = nullptr, down = nullptr;

@@ -91,9 +91,12 @@ __device__ void refine_store(const DevBatch& B, int p, const BodyRef& ra, const 
   if (B.status) B.status[p] |= g.status;
   if (B.mode == kModeGjkEpa) {
     if (gjk_contact(g)) {
-      const int bucket = bucket_of(ra.n > rb.n ? ra.n : rb.n);
-      const int e = atomicAdd(B.counts + kCntEpa + bucket, 1);
-      B.elists[(size_t)bucket * B.npairs + e] = p;
+      // the FP32 pass called it separated: a contact within rounding of the boundary,
+      // for the certified full-capacity pass over the late list (filled from the end of
+      // the spill array: these pairs are not contacts of the FP32 pass, so both lists
+      // together hold at most npairs entries)
+      const int q = atomicAdd(B.counts + kCntSpillLate, 1);
+      B.spill[B.npairs - 1 - q] = p | kSpill64;
     } else {
       store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
     }
@@ -262,27 +265,28 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
 
 // EPA at full capacity over the spill list: contacts that ran out of the small working
 // set, and -- certified, every face plane from FP64, exact supports -- contacts whose FP32
-// expansion met an inconsistent horizon or stopped short of the FP32 rounding level.
-// One warp per contact, points read from memory (any body size).
-__global__ void __launch_bounds__(128) k_epa_spill(DevBatch B) {
+// expansion met an inconsistent horizon or stopped short of the FP32 rounding level; or
+// (late != 0) over the contacts the FP64 refinement found, all certified.  One warp per
+// contact, points read from memory (any body size).
+__global__ void __launch_bounds__(128) k_epa_spill(DevBatch B, int late) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMemCert* mem = reinterpret_cast<EpaMemCert*>(smem_raw);
   const WarpTeam<32> t;
   EpaMemCert& M = mem[threadIdx.x / 32];
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int nteams = (gridDim.x * blockDim.x) / 32;
-  const int cnt = B.counts[kCntSpill];
+  const int cnt = B.counts[late ? kCntSpillLate : kCntSpill];
   Config cfg64 = B.cfg;
   cfg64.flags |= OGX_F_EPA_FP64_PLANES;
   for (int j = team; j < cnt; j += nteams) {
-    const int e = B.spill[j];
+    const int e = late ? B.spill[B.npairs - 1 - j] : B.spill[j];
     epa_item<32, 0, true>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
     t.sync();
   }
 }
 
-cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st) {
-  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B);
+cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st, bool late) {
+  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B, late ? 1 : 0);
   return cudaGetLastError();
 }
 

@@ -52,7 +52,8 @@ constexpr int kCntRefine = 2 * kBuckets + 1;  // separated pairs to refine in FP
 constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to continue in FP64
 constexpr int kCntSpill = 2 * kBuckets + 3;  // contacts that outgrew the small EPA capacity
 constexpr int kCntRefineBig = 2 * kBuckets + 4;  // of the FP64 continuations, bodies > 128 points
-constexpr int kCntSlots = 2 * kBuckets + 5;
+constexpr int kCntSpillLate = 2 * kBuckets + 5;  // contacts found by the FP64 refinement
+constexpr int kCntSlots = 2 * kBuckets + 6;
 // FP64 continuations of pairs whose bodies have at most this many points run one thread
 // per pair (FP64 instructions then serve 32 pairs); larger ones one warp per pair
 constexpr int kRefineLaneMax = 128;
@@ -313,7 +314,7 @@ int epa_variants_c(const KernelInfo** out);
 // non-template kernels (ogx_k_misc.cu)
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st, cudaStream_t st2,
                           cudaEvent_t routed);
-cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st);
+cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st, bool late = false);
 cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);
 cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,

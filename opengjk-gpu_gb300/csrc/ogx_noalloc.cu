@@ -190,6 +190,7 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = launch_epa_spill(B, S->grid_spill, s);
+  if (e == cudaSuccess) e = launch_epa_spill(B, S->grid_spill, s, true);
   if (e == cudaSuccess && (c.flags & OGX_F_FP64_POLISH)) e = launch_polish(B, S->grid_polish, s);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "no-allocation pipeline launch");
   return OGX_OK;

@@ -60,6 +60,7 @@ constexpr int kStreamMaxRanges = 64;
 constexpr int kStreamMaxLanes = 8;
 constexpr int kStreamLanes = 4;
 constexpr int kLaneForkConnections = 16;
+constexpr int kLaneForkWidth = 2;
 
 ogx_status ensure_streams(ogx_ctx* c, int nev) {
   cudaError_t e;
@@ -92,11 +93,15 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
   while (!s && (int)ctx->sub.size() < S) {
     ogx_ctx* c = nullptr;
     s = ogx_ctx_create(ctx->device, &ctx->cfg, nullptr, &c);
-    if (!s) ctx->sub.push_back(c);
+    if (!s) {
+      c->fork_width = kLaneForkWidth;
+      ctx->sub.push_back(c);
+    }
   }
-  // a lane also spreads its size buckets over streams of its own, when the process has
-  // enough hardware work queues for them; with the runtime's default of 8 the ~35 streams
-  // would share queues and serialise behind one another
+  // a lane also spreads its size buckets over two streams of its own (plus one for the
+  // FP64 refinement), when the process has enough hardware work queues for them: with
+  // the runtime's default of 8, or with more streams than queues, the copy streams would
+  // share a queue with a lane's kernels and wait behind them behind one another
   const char* conn_env = std::getenv("CUDA_DEVICE_MAX_CONNECTIONS");
   const bool lane_fork = conn_env && std::atoi(conn_env) >= kLaneForkConnections;
   for (int i = 0; !s && i < S; ++i) {

@@ -46,9 +46,11 @@ void one(const Job& J, int i, Work& M) {
   // same order as the device pipeline: the contact decision is taken on the FP32 GJK
   // result, separated pairs are then re-solved in FP64, contacts go through EPA
   bool contact = gjk_contact(g);
+  bool late = false;  // a contact only the FP64 refinement found
   if (g.polish) {
     gjk_refine(t, B, g, 16);
     contact = gjk_contact(g);
+    late = contact;
   }
   gkSimplex& s = J.smp[i];
   s.nvrtx = g.n;
@@ -65,9 +67,15 @@ void one(const Job& J, int i, Work& M) {
   int st = g.status, ei = 0;
   if (J.mode == 2) {
     if (contact) {
-      // as on the device: the small working set first, full capacity when it runs out
+      // as on the device: the small working set first, full capacity when it runs out;
+      // contacts found by the refinement go straight to the certified full pass
       EpaOut o;
-      epa_pair(t, B, *J.cfg, g, M.small, o, true);
+      if (late) {
+        o.spill = true;
+        o.spill64 = true;
+      } else {
+        epa_pair(t, B, *J.cfg, g, M.small, o, true);
+      }
       if (o.spill) {
         ogx_config c = *J.cfg;
         if (o.spill64) c.flags |= OGX_F_EPA_FP64_PLANES;
