@@ -667,8 +667,12 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     }
     return r;
   };
+  // Every bucket stream starts after the binning.  EPA bucket b takes only the contacts of
+  // GJK bucket b, so it follows that kernel on the same stream instead of waiting for every
+  // GJK bucket; the context's stream waits for all GJK buckets (the refinement needs them).
+  e = fork_out();
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "bucket fork");
   if (mode != kModeEpa) {
-    e = fork_out();
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
       const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
@@ -685,7 +689,6 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   // everything joins back into the context's stream.
   const bool refine = mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH);
   if (mode != kModeGjk) {
-    e = fork_out();
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
       const Launch& k = g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
