@@ -595,9 +595,11 @@ def run_ours(args):
             if e2e:
                 line["plain_form"]["engine_e2e_speedup"] = e2e["value"] / line["plain_form"]["e2e"]["value"]
     if not args.no_serving:
+        # the server brings its own contexts: release this one (its streams included)
         graph.close()
         del out, pairs
         pool.close()
+        ctx.close()
         torch.cuda.empty_cache()
         line["serving"] = serving_report(local)
     print(json.dumps(line), flush=True)

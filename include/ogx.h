@@ -350,6 +350,13 @@ ogx_status ogx_server_poll(ogx_server* server, int64_t ticket, int* done);
 /* Wait for a request (timeout_s <= 0: no limit); latency_ms = completion - submission
  * on the host clock.  The ticket is released. */
 ogx_status ogx_server_wait(ogx_server* server, int64_t ticket, double timeout_s, double* latency_ms);
+/* ogx_server_wait, plus where the latency went (phases_ms[4], may be NULL): [0] queued
+ * (submit to admission to a slot), [1] host staging of the pairs before the first copy,
+ * [2] device (first copy to results in host memory, CUDA events), [3] the rest (waiting
+ * for the version's world copy, launch issue not hidden by the device, completion
+ * detection). */
+ogx_status ogx_server_wait_phases(ogx_server* server, int64_t ticket, double timeout_s, double* latency_ms,
+                                  double* phases_ms);
 /* Device layout of the world-space pool of a version (for checks and custom kernels). */
 ogx_status ogx_server_world_layout(ogx_server* server, int64_t version, float** d_points,
                                    void** d_bodies);

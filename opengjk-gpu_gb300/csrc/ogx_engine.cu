@@ -124,8 +124,21 @@ bool serves(const Launch& v, int b) {
   return cap >= kBucketCap[b] && cap <= 8 * kBucketCap[b];
 }
 
-// default choice before tuning: one pair per warp, fewest registers that fit
-int default_choice(const std::vector<Launch>& vs, int b) {
+// Default choice before tuning: the variants the autotuner picks on this GPU for the
+// 1M-pair power-law batch (the same per bucket across runs): (lanes, K code) per bucket,
+// K code = register blocks + (resident blocks per SM << kOccShift).
+constexpr int kDefaultGjk[kBuckets][2] = {{1, 4}, {1, 5 << kOccShift}, {2, 4 << kOccShift}, {2, 4 << kOccShift},
+                                          {4, 4 << kOccShift}, {8, 4 << kOccShift}, {8, 4 << kOccShift}};
+constexpr int kDefaultEpa[kBuckets][2] = {{8, 1 + (5 << kOccShift)}, {8, 1 + (5 << kOccShift)},
+                                          {8, 2 + (5 << kOccShift)}, {8, 5 << kOccShift},
+                                          {8, 5 << kOccShift},     {8, 5 << kOccShift},
+                                          {16, 5 << kOccShift}};
+
+// otherwise one pair per warp, fewest registers that fit
+int default_choice(const std::vector<Launch>& vs, int b, bool epa) {
+  const int* want = epa ? kDefaultEpa[b] : kDefaultGjk[b];
+  for (int i = 0; i < (int)vs.size(); ++i)
+    if (vs[i].L == want[0] && vs[i].K == want[1] && serves(vs[i], b)) return i;
   int best = -1;
   for (int i = 0; i < (int)vs.size(); ++i) {
     if (!serves(vs[i], b) || vs[i].L != 32) continue;
@@ -214,8 +227,8 @@ ogx_status init_kernels(int device) {
 void set_defaults(ogx_ctx* ctx) {
   const bool tuned = ctx->device < 16 && g_tuned_valid[ctx->device];
   for (int b = 0; b < kBuckets; ++b) {
-    ctx->choice[0][b] = tuned ? g_tuned[ctx->device][0][b] : default_choice(g_gjkv, b);
-    ctx->choice[1][b] = tuned ? g_tuned[ctx->device][1][b] : default_choice(g_epav, b);
+    ctx->choice[0][b] = tuned ? g_tuned[ctx->device][0][b] : default_choice(g_gjkv, b, false);
+    ctx->choice[1][b] = tuned ? g_tuned[ctx->device][1][b] : default_choice(g_epav, b, true);
   }
 }
 

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -135,6 +136,8 @@ struct Request {
   float* out_nrm = nullptr;
   int32_t* out_status = nullptr;
   Clock::time_point t_submit, t_done;
+  Clock::time_point t_admit, t_staged;  // admitted to a slot; host staging done, first copy queued
+  float device_ms = -1.0f;             // first device operation to results in host memory
   int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
   ogx_status err = OGX_OK;
   // broad-phase request: the pairs come from the device grid of the version's world copy
@@ -170,6 +173,7 @@ struct Slot {
   float* h_nrm = nullptr;
   int32_t* h_status = nullptr;
   cudaEvent_t done = nullptr;
+  cudaEvent_t start = nullptr;  // the request's first device operation (timing)
   Request* req = nullptr;
   int world = -1;
   bool direct[5] = {};  // results copied straight into the caller's (pinned) arrays
@@ -245,9 +249,13 @@ bool ogx_server::admit(Request* r, Slot& s, int w) {
   }
   s.req = r;
   s.world = w;
+  r->t_admit = Clock::now();
   if (!r->broad) {
     std::memcpy(s.h_pairs, r->pairs.data(), r->npairs * sizeof(gkCollisionPair));
-    e = cudaMemcpyAsync(s.d_pairs, s.h_pairs, r->npairs * sizeof(gkCollisionPair), cudaMemcpyHostToDevice, st);
+    r->t_staged = Clock::now();
+    e = cudaEventRecord(s.start, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(s.d_pairs, s.h_pairs, r->npairs * sizeof(gkCollisionPair), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) {
       r->err = ogx_cuda_fail(e, "server request launch");
       return false;
@@ -256,6 +264,12 @@ bool ogx_server::admit(Request* r, Slot& s, int w) {
   }
   // stage 1: pairs from the grid, count back to the host
   const int cap = std::min(r->max_pairs, sc.slot_pairs);
+  r->t_staged = r->t_admit;
+  e = cudaEventRecord(s.start, st);
+  if (e != cudaSuccess) {
+    r->err = ogx_cuda_fail(e, "server broad phase");
+    return false;
+  }
   ogx_status os = broad_run(s.broad, st, d_world[w], local->d_bodies, local->nbodies, r->cell, r->margin, cap,
                             s.d_pairs, s.d_bres);
   if (os) {
@@ -362,6 +376,8 @@ void ogx_server::loop() {
         if (q == cudaErrorNotReady) continue;
         if (q == cudaSuccess) {
           finish(s);
+          float ms = -1.0f;
+          if (cudaEventElapsedTime(&ms, s.start, s.done) == cudaSuccess) r->device_ms = ms;
           r->state = 2;
         } else {
           r->err = ogx_cuda_fail(q, "server request");
@@ -440,6 +456,7 @@ void ogx_server::release() {
     cudaFreeHost(s.h_nrm);
     cudaFreeHost(s.h_status);
     if (s.done) cudaEventDestroy(s.done);
+    if (s.start) cudaEventDestroy(s.start);
     if (s.broad) ogx_broad_destroy(s.broad);
     cudaFree(s.d_bres);
     cudaFreeHost(s.h_bres);
@@ -515,11 +532,20 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
     S->world_version.push_back(-1);
     S->world_refs.push_back(0);
   }
+  // Slots spread their size buckets over streams of their own only as far as the
+  // process's hardware work queues go (CUDA_DEVICE_MAX_CONNECTIONS, 8 by default): a
+  // slot needs its own stream, the refinement's and the bucket streams, and streams
+  // beyond the queue count share queues and serialise behind unrelated work.
+  const char* conn_env = std::getenv("CUDA_DEVICE_MAX_CONNECTIONS");
+  const int conn = conn_env ? std::max(1, std::atoi(conn_env)) : 8;
+  const int per_slot = (conn - 2) / sc.slots;  // two queues kept for the server's own streams
   for (int i = 0; !st && i < sc.slots; ++i) {
     S->slots.emplace_back();
     Slot& s = S->slots.back();
     st = ogx_ctx_create(S->device, &S->cfg, nullptr, &s.ctx);
     if (st) break;
+    s.ctx->fork_ok = per_slot >= 4;
+    s.ctx->fork_width = std::min(kBuckets, std::max(2, per_slot - 2));
     for (int k = 0; k < 2; ++k)
       for (int b = 0; b < kBuckets; ++b) s.ctx->choice[k][b] = S->pctx->choice[k][b];
     const size_t n = sc.slot_pairs;
@@ -529,7 +555,7 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
         (e = halloc(&s.h_pairs, n)) != cudaSuccess || (e = halloc(&s.h_smp, n)) != cudaSuccess ||
         (e = halloc(&s.h_dist, n)) != cudaSuccess || (e = halloc(&s.h_nrm, 3 * n)) != cudaSuccess ||
         (e = halloc(&s.h_status, n)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming)) != cudaSuccess) {
+        (e = cudaEventCreate(&s.done)) != cudaSuccess || (e = cudaEventCreate(&s.start)) != cudaSuccess) {
       st = ogx_cuda_fail(e, "server slot buffers");
       break;
     }
@@ -651,6 +677,11 @@ extern "C" ogx_status ogx_server_submit(ogx_server* S, int64_t version, int npai
 }
 
 extern "C" ogx_status ogx_server_wait(ogx_server* S, int64_t ticket, double timeout_s, double* latency_ms) {
+  return ogx_server_wait_phases(S, ticket, timeout_s, latency_ms, nullptr);
+}
+
+extern "C" ogx_status ogx_server_wait_phases(ogx_server* S, int64_t ticket, double timeout_s, double* latency_ms,
+                                             double* phases_ms) {
   if (!S) return ogx_fail(OGX_ERR_INVALID, "NULL server");
   std::unique_lock<std::mutex> lk(S->mu);
   auto it = S->reqs.find(ticket);
@@ -663,7 +694,18 @@ extern "C" ogx_status ogx_server_wait(ogx_server* S, int64_t ticket, double time
       return ogx_fail(OGX_ERR_BUSY, "request %lld not done", (long long)ticket);
   }
   const ogx_status err = r->state == 3 ? r->err : OGX_OK;
-  if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  auto ms = [](Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+  };
+  const double lat = ms(r->t_submit, r->t_done);
+  if (latency_ms) *latency_ms = lat;
+  if (phases_ms) {
+    const bool ran = r->state == 2 && r->npairs > 0;
+    phases_ms[0] = ran ? ms(r->t_submit, r->t_admit) : 0.0;
+    phases_ms[1] = ran ? ms(r->t_admit, r->t_staged) : 0.0;
+    phases_ms[2] = ran ? (double)r->device_ms : 0.0;
+    phases_ms[3] = ran ? lat - phases_ms[0] - phases_ms[1] - phases_ms[2] : 0.0;
+  }
   S->reqs.erase(it);
   delete r;
   return err;

@@ -42,6 +42,9 @@ def _bind(lib):
     lib.ogx_server_poll.argtypes = [P, I64, ctypes.POINTER(ctypes.c_int)]
     lib.ogx_server_wait.restype = ctypes.c_int
     lib.ogx_server_wait.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]
+    lib.ogx_server_wait_phases.restype = ctypes.c_int
+    lib.ogx_server_wait_phases.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]
     lib.ogx_server_world_layout.restype = ctypes.c_int
     lib.ogx_server_world_layout.argtypes = [P, I64, ctypes.POINTER(P), ctypes.POINTER(P)]
     lib._ogx_server_bound = True
@@ -73,6 +76,7 @@ class Request:
         self.normal = arr(np.float32, (n, 3))
         self.status = arr(np.int32, (n,))
         self.latency_ms = None
+        self.phases_ms = None
         self.count = None  # broad-phase requests: [pairs found, error flags]
 
     def results(self) -> dict:
@@ -152,11 +156,15 @@ class Server:
         return bool(d.value)
 
     def wait(self, req: Request, timeout_s: float = 60.0) -> Request:
+        """Block until the request is done; sets req.latency_ms (submit to results in host
+        memory) and req.phases_ms (queued, host staging, device, rest)."""
         lat = ctypes.c_double()
-        rc = self.lib.ogx_server_wait(self.handle, req.ticket, float(timeout_s), ctypes.byref(lat))
+        ph = (ctypes.c_double * 4)()
+        rc = self.lib.ogx_server_wait_phases(self.handle, req.ticket, float(timeout_s), ctypes.byref(lat), ph)
         self._live.pop(req.ticket, None)
         _lib.check(rc)
         req.latency_ms = lat.value
+        req.phases_ms = tuple(ph)
         return req
 
     def world_layout(self, version: int):
