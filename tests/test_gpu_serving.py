@@ -141,3 +141,18 @@ def test_broadphase_request_matches_engine(scene, engine):
     ctx.synchronize()
     assert np.array_equal(req.dist[:n], ref["dist"])
     assert np.array_equal(req.normal[:n], ref["normal"])
+
+
+def test_latency_phases(scene):
+    """The latency breakdown of a request adds up: queued, staging, device and the rest
+    are non-negative (the rest within clock skew) and sum to the latency."""
+    pairs = scene.candidate_pairs(4, 20000)
+    with _server(scene) as srv:
+        for t in range(3):
+            v = srv.set_transforms(scene.transforms(4 + t))
+            req = srv.wait(srv.submit(v, pairs))
+            q, stg, dev, rest = req.phases_ms
+            assert q >= 0 and stg >= 0 and dev > 0, req.phases_ms
+            assert rest > -0.05, req.phases_ms
+            assert abs(q + stg + dev + rest - req.latency_ms) < 1e-6
+            assert dev <= req.latency_ms + 0.05
