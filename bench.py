@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop report")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip timing the reference's own GPU kernels on the same workload")
-    ap.add_argument("--chunks", type=int, default=8, help="pieces of the end-to-end streamed call")
+    ap.add_argument("--chunks", type=int, default=6, help="pieces of the end-to-end streamed call")
     ap.add_argument("--profile-launches", action="store_true",
                     help="one untimed step only (for ncu launch lists)")
     return ap.parse_args()
