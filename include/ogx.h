@@ -93,6 +93,8 @@ const char* ogx_version(void);
 /* ------------------------------------------------------------------------- */
 /* Engine API                                                                 */
 
+/* Pools, graphs and broad-phase objects refer to the context they were created with:
+ * destroy them before that context. */
 typedef struct ogx_ctx ogx_ctx;
 typedef struct ogx_pool ogx_pool;
 
@@ -144,6 +146,14 @@ int ogx_ctx_last_launches(const ogx_ctx* ctx);
  * fills up to cap (name, milliseconds) entries; returns the number filled. */
 ogx_status ogx_ctx_set_timing(ogx_ctx* ctx, int on);
 int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms, int cap);
+/* Stage timeline of the concurrent (forked) launches, for finding the chain that sets a
+ * call's duration: with it on, each call records an event after every bucket's GJK and
+ * EPA kernel on that bucket's stream and after the refinement, the late pass, the spill
+ * pass, the polish pass and the final join.  ogx_ctx_stage_timeline waits for the last
+ * call and fills up to cap (name, ms from the call's start) entries; returns the number
+ * filled.  Not recorded while a graph is being captured or with per-kernel timing on. */
+ogx_status ogx_ctx_set_stage_timeline(ogx_ctx* ctx, int on);
+int ogx_ctx_stage_timeline(ogx_ctx* ctx, const char** names, float* ms, int cap);
 /* Work counts of the last call (waits for it): pairs per GJK bucket [0, 7), contacts
  * per EPA bucket [7, 14), EPA faces re-solved in FP64 [14], pairs whose GJK result was
  * refined in FP64 [15], of which continued in FP64 (uncertain FP32 support) [16],

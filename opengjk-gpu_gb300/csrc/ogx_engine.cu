@@ -308,6 +308,8 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
   ctx->free_scratch();
   for (int i = 0; i <= ogx_ctx::kMaxTimed; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (int i = 0; i <= ogx_ctx::kMaxStages; ++i)
+    if (ctx->stage_ev[i]) cudaEventDestroy(ctx->stage_ev[i]);
   if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
   if (ctx->d_stage) cudaFree(ctx->d_stage);
   if (ctx->up) {
@@ -332,6 +334,7 @@ extern "C" ogx_status ogx_ctx_destroy(ogx_ctx* ctx) {
     cudaStreamSynchronize(ctx->aux_r);
     cudaStreamDestroy(ctx->aux_r);
   }
+
   if (ctx->route_ev) cudaEventDestroy(ctx->route_ev);
   if (ctx->rjoin_ev) cudaEventDestroy(ctx->rjoin_ev);
   cudaFree(ctx->d_io_pairs);
@@ -407,6 +410,34 @@ extern "C" int ogx_ctx_kernel_times(ogx_ctx* ctx, const char** names, float* ms,
   for (int i = 0; i < n; ++i) {
     if (names) names[i] = ctx->ev_name[i];
     if (ms) cudaEventElapsedTime(&ms[i], ctx->ev[i], ctx->ev[i + 1]);
+  }
+  return n;
+}
+
+extern "C" ogx_status ogx_ctx_set_stage_timeline(ogx_ctx* ctx, int on) {
+  if (!ctx) return ogx_fail(OGX_ERR_INVALID, "ctx is NULL");
+  cudaSetDevice(ctx->device);
+  if (on && !ctx->stage_ev[0]) {
+    for (int i = 0; i <= ogx_ctx::kMaxStages; ++i) {
+      cudaError_t e = cudaEventCreate(&ctx->stage_ev[i]);
+      if (e != cudaSuccess) return ogx_cuda_fail(e, "cudaEventCreate");
+    }
+  }
+  ctx->stages = on != 0;
+  ctx->stage_count = 0;
+  return OGX_OK;
+}
+
+extern "C" int ogx_ctx_stage_timeline(ogx_ctx* ctx, const char** names, float* ms, int cap) {
+  if (!ctx || !ctx->stages || ctx->stage_count == 0) return 0;
+  if (cudaEventSynchronize(ctx->stage_ev[ctx->stage_count]) != cudaSuccess) return -1;
+  const int n = std::min(cap, ctx->stage_count);
+  for (int i = 0; i < n; ++i) {
+    if (names) names[i] = ctx->stage_name[i];
+    if (ms) {
+      cudaEventSynchronize(ctx->stage_ev[1 + i]);
+      cudaEventElapsedTime(&ms[i], ctx->stage_ev[0], ctx->stage_ev[1 + i]);
+    }
   }
   return n;
 }
@@ -664,6 +695,19 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   // the others' work; with per-kernel timing on they run in sequence.
   const bool fork = !ctx->timing && ctx->fork_ok && ctx->ensure_aux() == OGX_OK;
   const int W = ctx->fork_width;  // bucket b runs on aux[b mod W]
+  // optional stage timeline of a forked call (not while a graph is being captured)
+  bool staged = false;
+  if (fork && ctx->stages && ctx->stage_ev[0]) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cs);
+    staged = cs == cudaStreamCaptureStatusNone && cudaEventRecord(ctx->stage_ev[0], st) == cudaSuccess;
+    ctx->stage_count = 0;
+  }
+  auto stage = [&](const char* name, cudaStream_t s2) {
+    if (!staged || ctx->stage_count >= ogx_ctx::kMaxStages) return;
+    if (cudaEventRecord(ctx->stage_ev[1 + ctx->stage_count], s2) == cudaSuccess)
+      ctx->stage_name[ctx->stage_count++] = name;
+  };
   auto bucket_stream = [&](int b) -> cudaStream_t { return fork ? ctx->aux[b % W] : st; };
   auto fork_out = [&]() -> cudaError_t {
     if (!fork) return cudaSuccess;
@@ -690,6 +734,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
       const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
       k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, 0, bucket_stream(b)>>>(B, b);
+      stage(kGjkName[b], bucket_stream(b));
       ++launches;
     }
     if (e == cudaSuccess) e = join_in();
@@ -706,25 +751,29 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
       const Launch& k = g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
       k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
+      stage(kEpaName[b], bucket_stream(b));
       ++launches;
     }
     if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA launches");
   }
+  const cudaStream_t rst = st;
   if (refine) {
     ctx->mark("refine");
-    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), st,
-                      fork ? ctx->aux_r : st, fork ? ctx->route_ev : nullptr);
+    e = launch_refine(B, fit_grid(g_grid_refine, npairs, 1), fit_grid(g_grid_pack, npairs, 1), rst,
+                      fork ? ctx->aux_r : rst, fork ? ctx->route_ev : nullptr);
     if (e == cudaSuccess && fork) {
       e = cudaEventRecord(ctx->rjoin_ev, ctx->aux_r);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->rjoin_ev, 0);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(rst, ctx->rjoin_ev, 0);
     }
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_refine launch");
+    stage("refine", rst);
     launches += 3;
     if (mode != kModeGjk) {
       // the contacts the refinement found (usually none), after it on the same stream
       ctx->mark("epa_late");
-      e = launch_epa_spill(B, fit_grid(g_grid_spill, std::max(1, npairs / 256), 32), st, true);
+      e = launch_epa_spill(B, fit_grid(g_grid_spill, std::max(1, npairs / 256), 32), rst, true);
       if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
+      stage("epa_late", rst);
       ++launches;
     }
   }
@@ -737,7 +786,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
       pst = ctx->aux[1];
       for (int b = 0; b < W && e == cudaSuccess; ++b) e = cudaEventRecord(ctx->join_ev[b], ctx->aux[b]);
       for (int b = 0; b < W && e == cudaSuccess; ++b) {
-        if (b != 0) e = cudaStreamWaitEvent(sst, ctx->join_ev[b], 0);
+        if (sst != ctx->aux[b]) e = cudaStreamWaitEvent(sst, ctx->join_ev[b], 0);
         if (e == cudaSuccess && b != 1) e = cudaStreamWaitEvent(pst, ctx->join_ev[b], 0);
       }
       if (e != cudaSuccess) return ogx_cuda_fail(e, "EPA join");
@@ -745,11 +794,13 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     ctx->mark("epa_spill");
     e = launch_epa_spill(B, fit_grid(g_grid_spill, npairs, 32), sst);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "k_epa_spill launch");
+    stage("epa_spill", sst);
     ++launches;
     if (ctx->cfg.flags & OGX_F_FP64_POLISH) {
       ctx->mark("polish");
       e = launch_polish(B, fit_grid(g_grid_polish, npairs, 1), pst);
       if (e != cudaSuccess) return ogx_cuda_fail(e, "k_polish launch");
+      stage("polish", pst);
       ++launches;
     }
     if (fork) {
@@ -762,6 +813,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return ogx_cuda_fail(e, "pipeline launch");
+  stage("end", st);
   if (ctx->timing) cudaEventRecord(ctx->ev[ctx->ev_count], st);
   ctx->last_launches = launches;
   return OGX_OK;

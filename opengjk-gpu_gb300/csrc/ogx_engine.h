@@ -58,6 +58,12 @@ struct ogx_ctx {
   int32_t* d_io_status = nullptr;
   size_t io_cap = 0;
   std::vector<float> stream_timeline;  // last streamed call with timing on (see ogx.h)
+  // stage timeline of forked calls (ogx_ctx_set_stage_timeline): events on the streams
+  bool stages = false;
+  static constexpr int kMaxStages = 40;
+  cudaEvent_t stage_ev[kMaxStages + 1] = {};  // [0] the call's start
+  const char* stage_name[kMaxStages] = {};
+  int stage_count = 0;
   std::vector<ogx_ctx*> sub;           // streamed calls: contexts running chunks side by side
 
   ogx_status ensure_scratch(int npairs);

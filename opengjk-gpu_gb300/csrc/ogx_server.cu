@@ -443,6 +443,9 @@ void ogx_server::loop() {
 
 void ogx_server::release() {
   for (Slot& s : slots) {
+    // the broad-phase scratch refers to the slot's context: release it first
+    if (s.broad) ogx_broad_destroy(s.broad);
+    s.broad = nullptr;
     if (s.ctx) ogx_ctx_destroy(s.ctx);
     cudaFree(s.d_pairs);
     cudaFree(s.d_smp);
@@ -457,7 +460,6 @@ void ogx_server::release() {
     cudaFreeHost(s.h_status);
     if (s.done) cudaEventDestroy(s.done);
     if (s.start) cudaEventDestroy(s.start);
-    if (s.broad) ogx_broad_destroy(s.broad);
     cudaFree(s.d_bres);
     cudaFreeHost(s.h_bres);
     if (s.counted) cudaEventDestroy(s.counted);

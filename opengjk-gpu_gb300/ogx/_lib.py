@@ -110,6 +110,8 @@ SIGNATURES = {
     "ogx_ctx_last_launches": (_I, [_P]),
     "ogx_ctx_set_timing": (_I, [_P, _I]),
     "ogx_ctx_kernel_times": (_I, [_P, _P, _P, _I]),
+    "ogx_ctx_set_stage_timeline": (_I, [_P, _I]),
+    "ogx_ctx_stage_timeline": (_I, [_P, _P, _P, _I]),
     "ogx_ctx_work_counts": (_I, [_P, _P, _I]),
     "ogx_ctx_get_kernel_choice": (_I, [_P, _I, _I, _P, _P]),
     "ogx_ctx_set_kernel_choice": (_I, [_P, _I, _I, _I, _I]),

@@ -17,9 +17,11 @@ from ._lib import SIMPLEX_DTYPE, check
 
 MODE_GJK, MODE_GJK_EPA, MODE_EPA = 1, 2, 3
 
-# Engine objects still open at exit are closed by an atexit hook (pools before their
-# contexts), while the CUDA runtime and torch are still intact; objects that are
-# garbage-collected during interpreter shutdown are left to the process exit.
+# Engine objects still open at exit are closed by an atexit hook (pools, graphs and
+# broad-phase objects before their contexts), while the CUDA runtime and torch are still
+# intact; objects that are garbage-collected during interpreter shutdown are left to the
+# process exit.  The C objects refer to their context, so a context closes its children
+# first, and a child whose context is already closed is not destroyed again.
 _live_pools: "weakref.WeakSet" = weakref.WeakSet()
 _live_ctxs: "weakref.WeakSet" = weakref.WeakSet()
 
@@ -67,7 +69,7 @@ class Context:
 
     def close(self):
         if self.handle:
-            for p in list(_live_pools):  # a pool cannot outlive its context
+            for p in list(_live_pools):  # pools, graphs, broad phases cannot outlive it
                 if p.ctx is self:
                     p.close()
             self.lib.ogx_ctx_destroy(self.handle)
@@ -112,6 +114,19 @@ class Context:
         n = self.lib.ogx_ctx_kernel_times(self.handle, names, ms, 32)
         if n < 0:
             raise _lib.OgxError(-2, "kernel timing failed")
+        return [(names[i].decode(), float(ms[i])) for i in range(n)]
+
+    def set_stage_timeline(self, on: bool = True):
+        check(self.lib.ogx_ctx_set_stage_timeline(self.handle, int(bool(on))))
+
+    def stage_timeline(self) -> list:
+        """[(stage, ms from the call's start)] of the last concurrent call (needs
+        set_stage_timeline(True))."""
+        names = (ctypes.c_char_p * 40)()
+        ms = (ctypes.c_float * 40)()
+        n = self.lib.ogx_ctx_stage_timeline(self.handle, names, ms, 40)
+        if n < 0:
+            raise _lib.OgxError(-2, "stage timeline failed")
         return [(names[i].decode(), float(ms[i])) for i in range(n)]
 
     def kernel_choice(self) -> dict:
@@ -367,6 +382,7 @@ class Graph:
                                        P(self.out.simplex.data_ptr()), P(self.out.dist.data_ptr()), nrm,
                                        P(self.out.status.data_ptr()), int(mode), ctypes.byref(h)))
         self.handle = h
+        _live_pools.add(self)
 
     @property
     def kernel_launches(self) -> int:
@@ -383,9 +399,9 @@ class Graph:
         return self.out
 
     def close(self):
-        if self.handle:
+        if self.handle and self.ctx.handle:
             self.ctx.lib.ogx_graph_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         if sys.is_finalizing():
@@ -405,6 +421,7 @@ class Broad:
         h = ctypes.c_void_p()
         check(ctx.lib.ogx_broad_create(ctx.handle, int(max_bodies), ctypes.byref(h)))
         self.handle = h
+        _live_pools.add(self)
         self._result = _torch().zeros(2, dtype=_torch().int32, device=f"cuda:{ctx.device}")
 
     def run(self, pool: Pool, cell: float, margin: float = 0.0, max_pairs: int = 1 << 20, pairs_dev=None):
