@@ -477,7 +477,7 @@ def run_ours(args):
                                  ("status", out.status))}
         d2h = sum(t.numel() * t.element_size() for t in host_out.values())
         h2d = coords_pinned.numel() * 4 + pairs_pinned.numel() * 4
-        e2e_steps = max(3, min(args.steps, 10))
+        e2e_steps = max(3, min(args.steps, 20))
 
         def e2e_step():
             # one public call from pinned host arrays to pinned host arrays
