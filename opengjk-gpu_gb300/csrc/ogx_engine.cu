@@ -733,7 +733,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
       const Launch& k = g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
-      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, 0, bucket_stream(b)>>>(B, b);
+      k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
       stage(kGjkName[b], bucket_stream(b));
       ++launches;
     }
