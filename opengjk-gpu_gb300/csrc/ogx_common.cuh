@@ -124,6 +124,76 @@ OGX_HD vec3<T> cvt(vec3<U> a) {
 typedef vec3<float> fv3;
 typedef vec3<double> dv3;
 
+// ----------------------------------------------------------------------------------
+// Double-float arithmetic: a value is the unevaluated sum hi + lo of two floats with
+// |lo| <= ulp(hi) / 2, about 48 significant bits.  It runs on the FP32 pipes, which issue
+// 64 times faster than FP64 on this part.  Error-free transformations: TwoSum (Knuth,
+// TAOCP vol. 2, 4.2.2), Fast2Sum and TwoProduct (Dekker, 1971, here with a fused
+// multiply-add); addition, multiplication and division as in the double-double
+// arithmetic of Hida, Li and Bailey (2001) with float parts.  Every step is an IEEE float
+// operation (no contraction), so host and device give the same bits.
+struct df {
+  float hi, lo;
+};
+OGX_HD df mk_df(float h, float l) {
+  df r;
+  r.hi = h;
+  r.lo = l;
+  return r;
+}
+OGX_HD df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return mk_df(s, (a - (s - bb)) + (b - bb));
+}
+OGX_HD df fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = a + b;
+  return mk_df(s, b - (s - a));
+}
+OGX_HD df two_prod(float a, float b) {
+  const float p = a * b;
+  return mk_df(p, fmaf(a, b, -p));
+}
+OGX_HD df operator+(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  const df t = two_sum(a.lo, b.lo);
+  s.lo += t.hi;
+  s = fast_two_sum(s.hi, s.lo);
+  s.lo += t.lo;
+  return fast_two_sum(s.hi, s.lo);
+}
+OGX_HD df operator-(df a) { return mk_df(-a.hi, -a.lo); }
+OGX_HD df operator-(df a, df b) { return a + (-b); }
+OGX_HD df operator*(df a, df b) {
+  df p = two_prod(a.hi, b.hi);
+  p.lo += a.hi * b.lo + a.lo * b.hi;
+  return fast_two_sum(p.hi, p.lo);
+}
+OGX_HD df operator/(df a, df b) {
+  const float q1 = a.hi / b.hi;
+  df r = a - b * mk_df(q1, 0.0f);
+  const float q2 = r.hi / b.hi;
+  r = r - b * mk_df(q2, 0.0f);
+  const float q3 = r.hi / b.hi;
+  return fast_two_sum(q1, q2) + mk_df(q3, 0.0f);
+}
+OGX_HD bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+OGX_HD bool operator>(df a, df b) { return b < a; }
+OGX_HD bool operator<=(df a, df b) { return !(b < a); }
+OGX_HD bool operator>=(df a, df b) { return !(a < b); }
+OGX_HD float to_float(df a) { return a.hi + a.lo; }
+OGX_HD float to_float(double a) { return (float)a; }
+// scalar constants and conversions for code written once for double and df
+template <class T>
+OGX_HD T sc(float x);
+template <>
+OGX_HD double sc<double>(float x) { return (double)x; }
+template <>
+OGX_HD df sc<df>(float x) { return mk_df(x, 0.0f); }
+typedef vec3<df> xv3;
+// exact difference of two float points as double-float components
+OGX_HD xv3 xdiff(fv3 a, fv3 b) { return v3<df>(two_sum(a.x, -b.x), two_sum(a.y, -b.y), two_sum(a.z, -b.z)); }
+
 // Support-scan dot product.  Written with explicit fused multiply-adds so that the
 // value of a vertex is the same wherever it is evaluated (scan, previous support).
 OGX_HD float sdot(float x, float y, float z, fv3 d) { return fmaf(z, d.z, fmaf(y, d.y, x * d.x)); }

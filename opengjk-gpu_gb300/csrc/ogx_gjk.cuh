@@ -360,76 +360,79 @@ OGX_HD void subdistance(Sx<T>& s, vec3<T>& dir, Unc& u) {
 // exact closest point of a simplex with <= 3 vertices to the origin, FP64
 // (region tests of Ericson, Real-Time Collision Detection, sec. 5.1.5, restated)
 
-OGX_HD void closest_on_simplex(int n, const dv3* P, double* lam, dv3& v) {
-  lam[0] = 1.0;
-  lam[1] = lam[2] = lam[3] = 0.0;
+template <class T>
+OGX_HD void closest_on_simplex_t(int n, const vec3<T>* P, T* lam, vec3<T>& v) {
+  const T zero = sc<T>(0.0f), one = sc<T>(1.0f);
+  lam[0] = one;
+  lam[1] = lam[2] = lam[3] = zero;
   if (n == 1) {
     v = P[0];
     return;
   }
   if (n == 2) {
-    const dv3 e = P[1] - P[0];
-    const double ee = dot(e, e);
-    double t = ee > 0.0 ? -dot(P[0], e) / ee : 0.0;
-    t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
-    lam[0] = 1.0 - t;
+    const vec3<T> e = P[1] - P[0];
+    const T ee = dot(e, e);
+    T t = ee > zero ? -dot(P[0], e) / ee : zero;
+    t = t < zero ? zero : (t > one ? one : t);
+    lam[0] = one - t;
     lam[1] = t;
     v = P[0] + e * t;
     return;
   }
-  const dv3 a = P[0], b = P[1], c = P[2];
-  const dv3 ab = b - a, ac = c - a;
-  const double d1 = -dot(ab, a), d2 = -dot(ac, a);
-  if (d1 <= 0.0 && d2 <= 0.0) {
+  const vec3<T> a = P[0], b = P[1], c = P[2];
+  const vec3<T> ab = b - a, ac = c - a;
+  const T d1 = -dot(ab, a), d2 = -dot(ac, a);
+  if (d1 <= zero && d2 <= zero) {
     v = a;
     return;
   }
-  const double d3 = -dot(ab, b), d4 = -dot(ac, b);
-  if (d3 >= 0.0 && d4 <= d3) {
-    lam[0] = 0.0;
-    lam[1] = 1.0;
+  const T d3 = -dot(ab, b), d4 = -dot(ac, b);
+  if (d3 >= zero && d4 <= d3) {
+    lam[0] = zero;
+    lam[1] = one;
     v = b;
     return;
   }
-  const double vc = d1 * d4 - d3 * d2;
-  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) {
-    const double t = d1 / (d1 - d3);
-    lam[0] = 1.0 - t;
+  const T vc = d1 * d4 - d3 * d2;
+  if (vc <= zero && d1 >= zero && d3 <= zero) {
+    const T t = d1 / (d1 - d3);
+    lam[0] = one - t;
     lam[1] = t;
     v = a + ab * t;
     return;
   }
-  const double d5 = -dot(ab, c), d6 = -dot(ac, c);
-  if (d6 >= 0.0 && d5 <= d6) {
-    lam[0] = 0.0;
-    lam[2] = 1.0;
+  const T d5 = -dot(ab, c), d6 = -dot(ac, c);
+  if (d6 >= zero && d5 <= d6) {
+    lam[0] = zero;
+    lam[2] = one;
     v = c;
     return;
   }
-  const double vb = d5 * d2 - d1 * d6;
-  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) {
-    const double t = d2 / (d2 - d6);
-    lam[0] = 1.0 - t;
+  const T vb = d5 * d2 - d1 * d6;
+  if (vb <= zero && d2 >= zero && d6 <= zero) {
+    const T t = d2 / (d2 - d6);
+    lam[0] = one - t;
     lam[2] = t;
     v = a + ac * t;
     return;
   }
-  const double va = d3 * d6 - d5 * d4;
-  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0) {
-    const double t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
-    lam[0] = 0.0;
-    lam[1] = 1.0 - t;
+  const T va = d3 * d6 - d5 * d4;
+  if (va <= zero && (d4 - d3) >= zero && (d5 - d6) >= zero) {
+    const T t = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+    lam[0] = zero;
+    lam[1] = one - t;
     lam[2] = t;
     v = b + (c - b) * t;
     return;
   }
-  const double den = 1.0 / (va + vb + vc);
-  const double s1 = vb * den, s2 = vc * den;
-  lam[0] = 1.0 - s1 - s2;
+  const T den = one / (va + vb + vc);
+  const T s1 = vb * den, s2 = vc * den;
+  lam[0] = one - s1 - s2;
   lam[1] = s1;
   lam[2] = s2;
   v = a + ab * s1 + ac * s2;
 }
+OGX_HD void closest_on_simplex(int n, const dv3* P, double* lam, dv3& v) { closest_on_simplex_t<double>(n, P, lam, v); }
 
 // --------------------------------------------------------------------------------
 // per-pair GJK
@@ -1037,8 +1040,66 @@ OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
   g.w1 = w1;
 }
 
+// The re-solve of a pair whose final simplex the FP32 pass proved final (its support is
+// certified), in double-float arithmetic on the FP32 pipes instead of FP64: the exact
+// Minkowski points a - b, the closest point of their simplex to about 48 bits, the
+// vertices it uses; then, as refine_end, FP32 witnesses and a correctly rounded distance.
+template <class Bodies>
+OGX_HD void refine_certain(const Bodies& B, GjkState& g) {
+  const int n0 = g.n > 3 ? 3 : g.n;
+  xv3 P[3];
+  int ia[3], ib[3];
+  for (int j = 0; j < n0; ++j) {
+    ia[j] = g.ia[j];
+    ib[j] = g.ib[j];
+    P[j] = xdiff(B.point(0, ia[j]), B.point(1, ib[j]));
+  }
+  df lam[4];
+  xv3 v;
+  closest_on_simplex_t<df>(n0, P, lam, v);
+  // keep the vertices the closest point uses (the single vertex of a point simplex)
+  int m = 0;
+  float ql[3] = {1.0f, 0.0f, 0.0f};
+  int qa[3] = {ia[0], 0, 0}, qb[3] = {ib[0], 0, 0};
+  xv3 Q[3];
+  Q[0] = P[0];
+  for (int j = 0; j < n0; ++j)
+    if (lam[j] > sc<df>(0.0f) || n0 == 1) {
+      Q[m] = P[j];
+      qa[m] = ia[j];
+      qb[m] = ib[j];
+      ql[m] = to_float(lam[j]);
+      ++m;
+    }
+  if (m == 0) {  // as the FP64 path: the first vertex alone
+    m = 1;
+    ql[0] = 1.0f;
+    v = P[0];
+  }
+  g.n = m;
+  for (int j = 0; j < m; ++j) {
+    g.ia[j] = qa[j];
+    g.ib[j] = qb[j];
+    g.P[j] = v3<float>(Q[j].x.hi, Q[j].y.hi, Q[j].z.hi);
+  }
+  g.status |= OGX_S_POLISHED;
+  fv3 w0 = v3<float>(0.f, 0.f, 0.f), w1 = w0;
+  for (int j = 0; j < m; ++j) {
+    w0 = w0 + B.point(0, qa[j]) * ql[j];
+    w1 = w1 + B.point(1, qb[j]) * ql[j];
+  }
+  g.v = v3<float>(to_float(v.x), to_float(v.y), to_float(v.z));
+  g.dist = sqrtf(to_float(dot(v, v)));
+  g.w0 = w0;
+  g.w1 = w1;
+}
+
 template <class Team, class Bodies>
 OGX_HD void gjk_refine(const Team& t, const Bodies& B, GjkState& g, int max_iter) {
+  if (g.certain) {
+    refine_certain(B, g);
+    return;
+  }
   RefineState r;
   refine_begin(B, g, max_iter, r);
   while (!r.done) {
