@@ -177,6 +177,13 @@ OGX_HD df operator/(df a, df b) {
   const float q3 = r.hi / b.hi;
   return fast_two_sum(q1, q2) + mk_df(q3, 0.0f);
 }
+// square root: one Newton step from the float root (Karp and Markstein's form)
+OGX_HD df df_sqrt(df a) {
+  if (!(a.hi > 0.0f)) return mk_df(0.0f, 0.0f);
+  const float x = sqrtf(a.hi);
+  const df r = a - two_prod(x, x);
+  return fast_two_sum(x, r.hi / (2.0f * x));
+}
 OGX_HD bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 OGX_HD bool operator>(df a, df b) { return b < a; }
 OGX_HD bool operator<=(df a, df b) { return !(b < a); }

@@ -238,56 +238,62 @@ OGX_HD void epa_touch(fv3 a, fv3 b, EpaOut& o) {
 // exact FP64 re-solve of the final face (plane, depth, witnesses)
 template <class Bodies>
 OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
-  dv3 A[3], Bq[3], Q[3];
+  // double-float arithmetic (about 48 bits) on the FP32 pipes: FP64 issues at 1/64 of
+  // the FP32 rate on this part, and the results are rounded to float
+  fv3 A[3], Bq[3];
+  xv3 Q[3];
   for (int k = 0; k < 3; ++k) {
-    A[k] = B.dpoint(0, o.face[k][0]);
-    Bq[k] = B.dpoint(1, o.face[k][1]);
-    Q[k] = A[k] - Bq[k];
+    A[k] = B.point(0, o.face[k][0]);
+    Bq[k] = B.point(1, o.face[k][1]);
+    Q[k] = xdiff(A[k], Bq[k]);
   }
-  const dv3 m = cross(Q[1] - Q[0], Q[2] - Q[0]);
-  const double mm = dot(m, m);
-  if (!(mm > 0.0)) return;
-  const double inv = 1.0 / sqrt(mm);
-  dv3 n = m * inv;
-  double d = dot(n, Q[0]);
+  const df zero = sc<df>(0.0f), one = sc<df>(1.0f);
+  const xv3 m = cross(Q[1] - Q[0], Q[2] - Q[0]);
+  const df mm = dot(m, m);
+  if (!(mm > zero)) return;
+  const df inv = one / df_sqrt(mm);
+  xv3 n = m * inv;
+  df d = dot(n, Q[0]);
   // keep the orientation chosen during the expansion
-  if (n.x * o.nrm.x + n.y * o.nrm.y + n.z * o.nrm.z < 0.0) {
+  if (n.x * sc<df>(o.nrm.x) + n.y * sc<df>(o.nrm.y) + n.z * sc<df>(o.nrm.z) < zero) {
     n = -n;
     d = -d;
   }
   // barycentric weights of the projection of the origin, clamped like tri_weights
-  const dv3 e0 = Q[1] - Q[0], e1 = Q[2] - Q[0];
-  const double d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1);
-  const double d20 = -dot(Q[0], e0), d21 = -dot(Q[0], e1);
-  const double den = d00 * d11 - d01 * d01;
-  double l[3] = {1.0 / 3.0, 1.0 / 3.0, 1.0 / 3.0};
-  if (fabs(den) > 0.0) {
-    const double u = (d11 * d20 - d01 * d21) / den;
-    const double v = (d00 * d21 - d01 * d20) / den;
-    const double w = 1.0 - u - v;
-    if (w < 0.0) {
-      const dv3 e12 = Q[2] - Q[1];
-      double tt = -dot(Q[1], e12) / dot(e12, e12);
-      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
-      l[0] = 0.0; l[1] = 1.0 - tt; l[2] = tt;
-    } else if (u < 0.0) {
-      double tt = -dot(Q[0], e1) / dot(e1, e1);
-      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
-      l[0] = 1.0 - tt; l[1] = 0.0; l[2] = tt;
-    } else if (v < 0.0) {
-      double tt = -dot(Q[0], e0) / dot(e0, e0);
-      tt = tt < 0.0 ? 0.0 : (tt > 1.0 ? 1.0 : tt);
-      l[0] = 1.0 - tt; l[1] = tt; l[2] = 0.0;
+  const xv3 e0 = Q[1] - Q[0], e1 = Q[2] - Q[0];
+  const df d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1);
+  const df d20 = -dot(Q[0], e0), d21 = -dot(Q[0], e1);
+  const df den = d00 * d11 - d01 * d01;
+  const df third = one / sc<df>(3.0f);
+  df l[3] = {third, third, third};
+  if (den.hi != 0.0f) {
+    const df u = (d11 * d20 - d01 * d21) / den;
+    const df v = (d00 * d21 - d01 * d20) / den;
+    const df w = one - u - v;
+    if (w < zero) {
+      const xv3 e12 = Q[2] - Q[1];
+      df tt = -dot(Q[1], e12) / dot(e12, e12);
+      tt = tt < zero ? zero : (tt > one ? one : tt);
+      l[0] = zero; l[1] = one - tt; l[2] = tt;
+    } else if (u < zero) {
+      df tt = -dot(Q[0], e1) / dot(e1, e1);
+      tt = tt < zero ? zero : (tt > one ? one : tt);
+      l[0] = one - tt; l[1] = zero; l[2] = tt;
+    } else if (v < zero) {
+      df tt = -dot(Q[0], e0) / dot(e0, e0);
+      tt = tt < zero ? zero : (tt > one ? one : tt);
+      l[0] = one - tt; l[1] = tt; l[2] = zero;
     } else {
       l[0] = w; l[1] = u; l[2] = v;
     }
   }
-  const dv3 w0 = A[0] * l[0] + A[1] * l[1] + A[2] * l[2];
-  const dv3 w1 = Bq[0] * l[0] + Bq[1] * l[1] + Bq[2] * l[2];
-  o.w0 = cvt<float>(w0);
-  o.w1 = cvt<float>(w1);
-  o.nrm = cvt<float>(n);
-  o.dist = (float)(-d);
+  auto lift = [](fv3 p) { return v3<df>(sc<df>(p.x), sc<df>(p.y), sc<df>(p.z)); };
+  const xv3 w0 = lift(A[0]) * l[0] + lift(A[1]) * l[1] + lift(A[2]) * l[2];
+  const xv3 w1 = lift(Bq[0]) * l[0] + lift(Bq[1]) * l[1] + lift(Bq[2]) * l[2];
+  o.w0 = v3<float>(to_float(w0.x), to_float(w0.y), to_float(w0.z));
+  o.w1 = v3<float>(to_float(w1.x), to_float(w1.y), to_float(w1.z));
+  o.nrm = v3<float>(to_float(n.x), to_float(n.y), to_float(n.z));
+  o.dist = to_float(-d);
   o.status |= OGX_S_POLISHED;
 }
 
