@@ -134,6 +134,9 @@ typedef vec3<double> dv3;
 // operation (no contraction), so host and device give the same bits.
 struct df {
   float hi, lo;
+  df() = default;
+  OGX_HD explicit df(int i) : hi((float)i), lo(0.0f) {}
+  OGX_HD explicit df(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
 };
 OGX_HD df mk_df(float h, float l) {
   df r;
@@ -163,6 +166,7 @@ OGX_HD df operator+(df a, df b) {
   return fast_two_sum(s.hi, s.lo);
 }
 OGX_HD df operator-(df a) { return mk_df(-a.hi, -a.lo); }
+OGX_HD df fabs(df a) { return a.hi < 0.0f ? mk_df(-a.hi, -a.lo) : a; }
 OGX_HD df operator-(df a, df b) { return a + (-b); }
 OGX_HD df operator*(df a, df b) {
   df p = two_prod(a.hi, b.hi);
@@ -188,6 +192,21 @@ OGX_HD bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo 
 OGX_HD bool operator>(df a, df b) { return b < a; }
 OGX_HD bool operator<=(df a, df b) { return !(b < a); }
 OGX_HD bool operator>=(df a, df b) { return !(a < b); }
+OGX_HD bool operator==(df a, df b) { return a.hi == b.hi && a.lo == b.lo; }
+OGX_HD df& operator+=(df& a, df b) { return a = a + b; }
+template <class T>
+OGX_HD T tmin(T a, T b) { return b < a ? b : a; }
+template <class T>
+OGX_HD T tmax(T a, T b) { return a < b ? b : a; }
+OGX_HD double tsqrt(double a) { return sqrt(a); }
+OGX_HD df tsqrt(df a) { return df_sqrt(a); }
+// unit roundoff-based floor factor of the arithmetic (2^-52 for double, 2^-47 for df)
+template <class T>
+OGX_HD double prec_eps();
+template <>
+OGX_HD double prec_eps<double>() { return DBL_EPSILON; }
+template <>
+OGX_HD double prec_eps<df>() { return 7.105427357601002e-15; }
 OGX_HD float to_float(df a) { return a.hi + a.lo; }
 OGX_HD float to_float(double a) { return (float)a; }
 // scalar constants and conversions for code written once for double and df
@@ -291,6 +310,8 @@ struct SerialTeam {
   OGX_HD void argmin(float&, int&) const {}
   OGX_HD void argmax2(float&, int&, float&) const {}
   OGX_HD void argmax_d(double&, int&) const {}
+  template <class T>
+  OGX_HD void argmax_t(T&, int&) const {}
   OGX_HD bool any(bool p) const { return p; }
   OGX_HD uint32_t ballot(bool p) const { return p ? 1u : 0u; }
   OGX_HD uint32_t below() const { return 0u; }
@@ -333,6 +354,18 @@ struct WarpTeam {
 #pragma unroll
     for (int o = L / 2; o > 0; o >>= 1) {
       const double v2 = __shfl_xor_sync(mask, v, o);
+      const int i2 = __shfl_xor_sync(mask, i, o);
+      if (v2 > v || (v2 == v && i2 < i)) {
+        v = v2;
+        i = i2;
+      }
+    }
+  }
+  __device__ void argmax_t(double& v, int& i) const { argmax_d(v, i); }
+  __device__ void argmax_t(df& v, int& i) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) {
+      const df v2 = mk_df(__shfl_xor_sync(mask, v.hi, o), __shfl_xor_sync(mask, v.lo, o));
       const int i2 = __shfl_xor_sync(mask, i, o);
       if (v2 > v || (v2 == v && i2 < i)) {
         v = v2;

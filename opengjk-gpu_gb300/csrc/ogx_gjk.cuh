@@ -822,10 +822,10 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
 // fl(x . d32) >= m - 2e with e >= |fl(x . d32) - x . d| <= 2 FLT_EPSILON |x|_max |d|_1
 // (rounding of d to FP32 plus the FP32 dot product), so only those few candidates are
 // evaluated in FP64.  Ties go to the lowest index.
-template <class Team, class Bodies>
-OGX_HD int exact_support(const Team& t, const Bodies& B, int w, dv3 d, double& val) {
+template <class Team, class Bodies, class T>
+OGX_HD int exact_support(const Team& t, const Bodies& B, int w, vec3<T> d, T& val) {
   const MemBodies& M = B.mem_view();
-  const fv3 fd = cvt<float>(d);
+  const fv3 fd = v3<float>(to_float(d.x), to_float(d.y), to_float(d.z));
   const float* X = M.base[w];
   const float* Y = X + M.n4[w];
   const float* Z = Y + M.n4[w];
@@ -839,20 +839,28 @@ OGX_HD int exact_support(const Team& t, const Bodies& B, int w, dv3 d, double& v
   amax = t.fmax_(amax);
   const float e = 4.0f * FLT_EPSILON * amax * (fabsf(fd.x) + fabsf(fd.y) + fabsf(fd.z)) + FLT_MIN;
   const float lo = m - 2.0f * e;
-  double best = -INFINITY;
+  T best = sc<T>(-INFINITY);
   int bi = 0x7fffffff;
   for (int i = t.lane(); i < n; i += Team::L) {
     if (sdot(X[i], Y[i], Z[i], fd) < lo) continue;
-    const double x = (double)X[i] * d.x + (double)Y[i] * d.y + (double)Z[i] * d.z;
+    const T x = sc<T>(X[i]) * d.x + sc<T>(Y[i]) * d.y + sc<T>(Z[i]) * d.z;
     if (x > best || (x == best && i < bi)) {
       best = x;
       bi = i;
     }
   }
-  t.argmax_d(best, bi);
+  t.argmax_t(best, bi);
   val = best;
   return bi;
 }
+
+// the Minkowski point a_i - b_j exactly (double), or as double-float components
+template <class T>
+struct Tag {};
+template <class Bodies>
+OGX_HD dv3 mpoint(Tag<double>, const Bodies& B, int i, int j) { return B.dpoint(0, i) - B.dpoint(1, j); }
+template <class Bodies>
+OGX_HD xv3 mpoint(Tag<df>, const Bodies& B, int i, int j) { return xdiff(B.point(0, i), B.point(1, j)); }
 
 // FP64 continuation of GJK from the FP32 result: exact supports, FP64 sub-distance,
 // stop when the FP64 gap |v|^2 - v.w <= 1e-12 |v|^2 or the support repeats.  Certifies
@@ -860,47 +868,56 @@ OGX_HD int exact_support(const Team& t, const Bodies& B, int w, dv3 d, double& v
 // Split in three so that a warp can run the supports of 32 pairs cooperatively while
 // each lane keeps its own pair's state (refine_begin, then refine_step with the exact
 // supports along -v / v until done, then refine_end).
-struct RefineState {
-  Sx<double> s;
+// written for double and double-float; the continuation runs in FP64: its progress
+// and gap tests need |v|^2 to about 1e-12 relative, and near-coplanar thin bodies put the
+// origin 1e-5 of the coordinates' scale from the simplex, where the 48 bits of
+// double-float leave |v|^2 with ~1e-10 relative noise (it stopped a step early on some
+// 1e-4-thick disks).  The one-shot re-solves (refine_certain, epa_polish) have no such
+// decision and run in double-float.
+template <class T>
+struct RefineStateT {
+  Sx<T> s;
   int ia[4], ib[4];
-  dv3 v;
-  double lam[4];   // barycentric weights of v on s (valid while no step changed s)
+  vec3<T> v;
+  T lam[4];   // barycentric weights of v on s (valid while no step changed s)
   bool lam_valid;
-  double wmax2;
+  T wmax2;
   int it, max_iter;
   bool done, enclosed;
 };
+typedef RefineStateT<double> RefineState;
 
-template <class Bodies>
-OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, RefineState& r) {
-  Sx<double>& s = r.s;
+template <class Bodies, class T>
+OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, RefineStateT<T>& r) {
+  Sx<T>& s = r.s;
+  const T zero = sc<T>(0.0f);
   s.n = g.n > 3 ? 3 : g.n;
   for (int j = 0; j < s.n; ++j) {
     r.ia[j] = g.ia[j];
     r.ib[j] = g.ib[j];
-    s.v[j].p = B.dpoint(0, r.ia[j]) - B.dpoint(1, r.ib[j]);
+    s.v[j].p = mpoint(Tag<T>(), B, r.ia[j], r.ib[j]);
     s.v[j].k = j;
   }
   // exact closest point of the FP32 result's simplex; keep only the vertices it uses
-  dv3 P[3];
+  vec3<T> P[3];
   for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
-  double lam[4];
-  closest_on_simplex(s.n, P, lam, r.v);
+  T lam[4];
+  closest_on_simplex_t<T>(s.n, P, lam, r.v);
   {
-    Sx<double> q;
+    Sx<T> q;
     q.n = 0;
     int qa[4], qb[4];
     for (int j = 0; j < s.n; ++j)
-      if (lam[j] > 0.0 || (s.n == 1)) {
+      if (lam[j] > zero || (s.n == 1)) {
         q.v[q.n] = s.v[j];
         qa[q.n] = r.ia[j];
         qb[q.n] = r.ib[j];
         q.n++;
       }
-    double ql[4] = {1.0, 0.0, 0.0, 0.0};
+    T ql[4] = {sc<T>(1.0f), zero, zero, zero};
     int m = 0;
     for (int j = 0; j < s.n; ++j)
-      if (lam[j] > 0.0 || (s.n == 1)) ql[m++] = lam[j];
+      if (lam[j] > zero || (s.n == 1)) ql[m++] = lam[j];
     r.lam_valid = q.n > 0;
     if (q.n == 0) {
       q.v[0] = s.v[0];
@@ -916,32 +933,32 @@ OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, Refin
       r.lam[j] = ql[j];
     }
   }
-  r.wmax2 = 0.0;
-  for (int j = 0; j < s.n; ++j) r.wmax2 = fmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
+  r.wmax2 = zero;
+  for (int j = 0; j < s.n; ++j) r.wmax2 = tmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
   r.max_iter = max_iter;
   r.enclosed = false;
   r.it = g.certain ? max_iter + 1 : 0;  // the FP32 pass proved the simplex final
   r.done = r.it >= max_iter;
 }
 
-// one FP64 iteration with the exact supports xa (body 1 along -v) and xb (body 2 along v)
-template <class Bodies>
-OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
-  Sx<double>& s = r.s;
-  const dv3 w = B.dpoint(0, xa) - B.dpoint(1, xb);
-  const double vv = dot(r.v, r.v);
+// one iteration with the exact supports xa (body 1 along -v) and xb (body 2 along v)
+template <class Bodies, class T>
+OGX_HD void refine_step(const Bodies& B, RefineStateT<T>& r, int xa, int xb) {
+  Sx<T>& s = r.s;
+  const vec3<T> w = mpoint(Tag<T>(), B, xa, xb);
+  const T vv = dot(r.v, r.v);
   // FP64 gap test.  In exact arithmetic v.p_j = |v|^2 for every vertex p_j of the
   // current feature, so the gap |v|^2 - v.w equals v.(p_j - w); that form rounds in
   // proportion to |p_j - w| (small near convergence) instead of |w|^2.  Relative
   // tolerance of the FP64 oracle (eps * 1e4) and a rounding floor.
-  double gap = INFINITY, dmax = 0.0;
+  T gap = sc<T>(INFINITY), dmax = sc<T>(0.0f);
   for (int j = 0; j < s.n; ++j) {
-    const dv3 e = s.v[j].p - w;
-    gap = fmin(gap, dot(r.v, e));
-    dmax = fmax(dmax, dot(e, e));
+    const vec3<T> e = s.v[j].p - w;
+    gap = tmin(gap, dot(r.v, e));
+    dmax = tmax(dmax, dot(e, e));
   }
-  const double floor64 = 4.0 * DBL_EPSILON * sqrt(r.wmax2) * sqrt(dmax);
-  if (gap <= 1e-12 * vv || gap <= floor64) {
+  const T floor64 = T(4.0 * prec_eps<T>()) * tsqrt(r.wmax2) * tsqrt(dmax);
+  if (gap <= T(1e-12) * vv || gap <= floor64) {
     r.done = true;
     return;
   }
@@ -951,13 +968,13 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
     r.done = true;
     return;
   }
-  const Sx<double> prev = s;
+  const Sx<T> prev = s;
   int pa[4], pb[4];
   for (int j = 0; j < s.n; ++j) {
     pa[j] = r.ia[j];
     pb[j] = r.ib[j];
   }
-  const dv3 vprev = r.v;
+  const vec3<T> vprev = r.v;
   s.v[s.n].p = w;
   s.v[s.n].k = s.n;
   r.ia[s.n] = xa;
@@ -966,7 +983,7 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
   Unc u{false};
   subdistance(s, r.v, u);
   r.lam_valid = false;
-  if (s.n != 4 && !(dot(r.v, r.v) < vv * (1.0 - 1e-12))) {
+  if (s.n != 4 && !(dot(r.v, r.v) < vv * T(1.0 - 1e-12))) {
     // no progress: a tie support spanning a degenerate simplex -- keep the last answer
     s = prev;
     r.v = vprev;
@@ -986,7 +1003,7 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
     r.ia[j] = na[j];
     r.ib[j] = nb[j];
     s.v[j].k = j;
-    r.wmax2 = fmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
+    r.wmax2 = tmax(r.wmax2, dot(s.v[j].p, s.v[j].p));
   }
   if (s.n == 4) {
     r.enclosed = true;
@@ -997,14 +1014,14 @@ OGX_HD void refine_step(const Bodies& B, RefineState& r, int xa, int xb) {
   if (r.it >= r.max_iter) r.done = true;
 }
 
-template <class Bodies>
-OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
-  const Sx<double>& s = r.s;
+template <class Bodies, class T>
+OGX_HD void refine_end(const Bodies& B, const RefineStateT<T>& r, GjkState& g) {
+  const Sx<T>& s = r.s;
   g.n = s.n;
   for (int j = 0; j < s.n; ++j) {
     g.ia[j] = r.ia[j];
     g.ib[j] = r.ib[j];
-    g.P[j] = cvt<float>(s.v[j].p);
+    g.P[j] = v3<float>(to_float(s.v[j].p.x), to_float(s.v[j].p.y), to_float(s.v[j].p.z));
   }
   g.status |= (r.it == r.max_iter + 1) ? OGX_S_POLISHED : (OGX_S_POLISHED | OGX_S_GJK_ESCALATED);
   if (r.it == r.max_iter) g.status |= OGX_S_GJK_CAP;
@@ -1013,16 +1030,16 @@ OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
     g.dist = 0.0f;
     return;
   }
-  double lam[4];
-  dv3 v;
+  T lam[4];
+  vec3<T> v;
   if (r.lam_valid) {
     // the simplex is the one refine_begin solved: reuse its closest point
     v = r.v;
     for (int j = 0; j < 4; ++j) lam[j] = r.lam[j];
   } else {
-    dv3 P[3];
+    vec3<T> P[3];
     for (int j = 0; j < s.n; ++j) P[j] = s.v[j].p;
-    closest_on_simplex(s.n, P, lam, v);
+    closest_on_simplex_t<T>(s.n, P, lam, v);
   }
   // The distance needs the FP64 closest point; its square root and the witnesses do
   // not: FP32 from here on (|v|^2 rounded once, then a correctly rounded sqrtf: 1 ulp;
@@ -1030,12 +1047,12 @@ OGX_HD void refine_end(const Bodies& B, const RefineState& r, GjkState& g) {
   // above).  FP64 issues at 1/64 of the FP32 rate here.
   fv3 w0 = v3<float>(0.f, 0.f, 0.f), w1 = w0;
   for (int j = 0; j < s.n; ++j) {
-    const float l = (float)lam[j];
+    const float l = to_float(lam[j]);
     w0 = w0 + B.point(0, r.ia[j]) * l;
     w1 = w1 + B.point(1, r.ib[j]) * l;
   }
-  g.v = cvt<float>(v);
-  g.dist = sqrtf((float)dot(v, v));
+  g.v = v3<float>(to_float(v.x), to_float(v.y), to_float(v.z));
+  g.dist = sqrtf(to_float(dot(v, v)));
   g.w0 = w0;
   g.w1 = w1;
 }

@@ -103,9 +103,9 @@ __device__ void refine_store(const DevBatch& B, int p, const BodyRef& ra, const 
   }
 }
 
-// FP64 re-solve of separated pairs (one thread per pair: the FP64 units see full
-// warps).  Pairs whose final support the GJK kernel proved exact only need the exact
-// closest point of their simplex; the others are passed to k_refine_full.
+// Re-solve of separated pairs (one thread per pair).  Pairs whose final support the GJK
+// kernel proved exact only need the exact closest point of their simplex, computed in
+// double-float arithmetic; the others are passed to k_refine_lane / k_refine_full.
 __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   const int cnt = B.counts[kCntRefine];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
