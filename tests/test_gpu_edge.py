@@ -219,3 +219,27 @@ def test_streamed_ranges_match_batched(engine, lanes):
             engine.streamed(ctx, pool, coords, pairs, bounds=bad, lanes=lanes)
     with pytest.raises(RuntimeError):
         engine.streamed(ctx, pool, coords, pairs, bounds=[0, 3000], lanes=9)
+
+
+def test_stage_timeline(engine):
+    """The stage timeline of a concurrent call names every bucket's GJK and EPA kernel and
+    the passes after them, with times from the call's start that end at the join; results
+    are unchanged by recording it."""
+    import torch
+    b = W.powerlaw(seed=46, n_pairs=20000)
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    pool.upload(b.coords)
+    pairs = torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()
+    ref = engine.run(ctx, pool, pairs).to_host()
+    ctx.set_stage_timeline(True)
+    got = engine.run(ctx, pool, pairs).to_host()
+    tl = dict(ctx.stage_timeline())
+    ctx.set_stage_timeline(False)
+    ctx.synchronize()
+    assert np.array_equal(got["dist"], ref["dist"])
+    names = {f"gjk{s}" for s in ("<=16", "<=32", "<=64", "<=128", "<=256", "<=512", ">512")}
+    names |= {n.replace("gjk", "epa") for n in names} | {"refine", "epa_late", "epa_spill", "polish", "end"}
+    assert set(tl) == names, sorted(tl)
+    assert all(0.0 <= v <= tl["end"] + 1e-3 for v in tl.values()), tl
+    assert tl["refine"] <= tl["epa_late"] + 1e-3
