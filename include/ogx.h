@@ -160,7 +160,9 @@ int ogx_ctx_stage_timeline(ogx_ctx* ctx, const char** names, float* ms, int cap)
  * contacts whose EPA outgrew the bucket kernels' working set and ran again at full
  * capacity [17], FP64 continuations of pairs with a body above 128 points (one warp
  * each; the others in [16] - [18] run one thread each) [18], contacts that only the
- * FP64 refinement found (certified full-capacity EPA) [19].  cap must be >= 20. */
+ * FP64 refinement found (certified full-capacity EPA) [19], capacity spills whose
+ * expansion the full-capacity pass continued instead of restarting [20] (at most 4096 per
+ * call).  cap must be >= 21. */
 int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap);
 
 /* Kernel variant per size bucket (bucket b holds pairs whose larger body has at most
@@ -171,8 +173,10 @@ ogx_status ogx_ctx_get_kernel_choice(const ogx_ctx* ctx, int kind, int bucket, i
                                      int* blocks);
 ogx_status ogx_ctx_set_kernel_choice(ogx_ctx* ctx, int kind, int bucket, int lanes, int blocks);
 /* Autotuner: times every compiled variant that can serve each bucket on this batch
- * (device buffers; `reps` runs per candidate, best time kept), keeps the fastest per
- * bucket for this context and for contexts created later on the same device.
+ * (device buffers; `reps` runs per candidate, kernels one after another, best time
+ * kept) and takes the fastest per bucket; since a call runs the buckets concurrently, it
+ * then times whole calls with that set and with the context's previous one and keeps
+ * the faster, for this context and for contexts created later on the same device.
  * Synchronous. */
 ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
                         const gkCollisionPair* d_pairs, int reps);

@@ -294,6 +294,8 @@ void ogx_ctx::free_scratch() {
   cudaFree(d_refine_full);
   cudaFree(d_spill);
   d_spill = nullptr;
+  cudaFree(d_resume);
+  d_resume = nullptr;
   d_refine = nullptr;
   d_refine_full = nullptr;
   d_lists = d_elists = d_counts = nullptr;
@@ -463,6 +465,7 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
       (e = cudaMalloc(&d_refine, cap * sizeof(RefineRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine_full, cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_spill, cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_resume, kResumeCap * sizeof(EpaResume))) != cudaSuccess ||
       (e = cudaMalloc(&d_counts, 64 * sizeof(int))) != cudaSuccess) {
     free_scratch();
     return ogx_cuda_fail(e, "scratch allocation");
@@ -672,6 +675,8 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.refine = ctx->d_refine;
   B.refine_full = ctx->d_refine_full;
   B.spill = ctx->d_spill;
+  B.resume = ctx->d_resume;
+  B.resume_cap = ogx_ctx::kResumeCap;
   B.warm = d_warm;
   B.subtab = g_subtab;
   B.cfg = ctx->cfg;
@@ -969,11 +974,11 @@ extern "C" ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npair
       rounds = std::max(rounds, (int)cands[kind][b].size());
     }
   float best[2][kBuckets];
-  int pick[2][kBuckets];
+  int pick[2][kBuckets], pick_prior[2][kBuckets];
   for (int kind = 0; kind < 2; ++kind)
     for (int b = 0; b < kBuckets; ++b) {
       best[kind][b] = INFINITY;
-      pick[kind][b] = ctx->choice[kind][b];
+      pick[kind][b] = pick_prior[kind][b] = ctx->choice[kind][b];
     }
   const bool was_timing = ctx->timing;
   ogx_status s = ogx_ctx_set_timing(ctx, 1);
@@ -1006,6 +1011,43 @@ extern "C" ogx_status ogx_autotune(ogx_ctx* ctx, const ogx_pool* pool, int npair
         }
       }
     }
+  }
+  // The candidates were timed one after another, but a call runs the buckets
+  // concurrently: keep the picked set only if a whole concurrent call with it is not
+  // slower than with the set the context started from (best of three each).
+  ogx_ctx_set_timing(ctx, 0);
+  auto whole_call = [&](int (*ch)[kBuckets], float* best_ms) -> ogx_status {
+    for (int kind = 0; kind < 2; ++kind)
+      for (int b = 0; b < kBuckets; ++b) ctx->choice[kind][b] = ch[kind][b];
+    *best_ms = INFINITY;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    ogx_status r = ce == cudaSuccess ? OGX_OK : ogx_cuda_fail(ce, "autotune events");
+    for (int k = 0; k < 4 && !r; ++k) {
+      cudaEventRecord(e0, ctx->stream);
+      r = ogx_run(ctx, pool->d_points, pool->d_bodies, pool->nbodies, npairs, d_pairs, smp, dist, nrm, nullptr,
+                  kModeGjkEpa);
+      cudaEventRecord(e1, ctx->stream);
+      float ms = 0.0f;
+      if (!r && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+          k > 0)  // the first run warms up
+        *best_ms = std::min(*best_ms, ms);
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return r;
+  };
+  if (!s) {
+    int prior[2][kBuckets];
+    for (int kind = 0; kind < 2; ++kind)
+      for (int b = 0; b < kBuckets; ++b) prior[kind][b] = pick_prior[kind][b];
+    float t_pick = INFINITY, t_prior = INFINITY;
+    s = whole_call(pick, &t_pick);
+    if (!s) s = whole_call(prior, &t_prior);
+    if (!s && t_prior < t_pick)
+      for (int kind = 0; kind < 2; ++kind)
+        for (int b = 0; b < kBuckets; ++b) pick[kind][b] = prior[kind][b];
   }
   ogx_ctx_set_timing(ctx, was_timing);
   cudaFree(smp);

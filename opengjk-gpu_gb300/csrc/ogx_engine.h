@@ -23,6 +23,8 @@ struct ogx_ctx {
   ogx::RefineRec* d_refine = nullptr;
   int* d_refine_full = nullptr;
   int* d_spill = nullptr;
+  ogx::EpaResume* d_resume = nullptr;  // kResumeCap saved expansions of capacity spills
+  static constexpr int kResumeCap = 4096;
   size_t cap_pairs = 0;
   // staging for host uploads
   void* h_stage = nullptr;

@@ -56,6 +56,27 @@ struct EpaMemCert : EpaMem {
   double4 fn64[kEpaFmax];  // unit outward normal and plane distance, FP64 from exact points
 };
 OGX_HD double4* plane64_slot(EpaMemCert& M, int f) { return &M.fn64[f]; }
+
+// A small-capacity expansion that ran out of room, kept for the full-capacity pass to
+// continue from instead of starting again: the polytope and the loop state at the top of
+// the iteration that overflowed.  The full pass makes the same decisions up to there (the
+// face slots do not depend on the capacity), so the result is the same as a restart.
+struct EpaResume {
+  int pair, nv, fend, it, st, status;
+  float scale2;
+  float4 fn[EpaMemSmall::kF];
+  float4 vp[EpaMemSmall::kV];
+  int2 vid[EpaMemSmall::kV];
+  uint8_t fv[EpaMemSmall::kF][4];
+  uint8_t fa[EpaMemSmall::kF][4];
+};
+// where a spilling expansion saves itself: cap records in buf, *count the next free one
+// (buf null or full: the full pass restarts the contact)
+struct EpaResumeSink {
+  EpaResume* buf;
+  int* count;
+  int cap;
+};
 template <class Mem>
 OGX_HD double4* plane64_slot(Mem&, int) { return nullptr; }
 
@@ -80,6 +101,7 @@ struct EpaOut {
   bool spill;      // ran out of (small) capacity: nothing written, run again at full capacity
   bool spill64;    // ... because the FP32 expansion met an inconsistent horizon: the re-run
                    // solves every face plane in FP64
+  int resume;      // a capacity spill saved to this EpaResume record (-1: none)
 };
 
 OGX_HD fv3 unit_or_x(fv3 d) {
@@ -297,6 +319,43 @@ OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
   o.status |= OGX_S_POLISHED;
 }
 
+template <class Team, class Mem>
+OGX_HD void epa_save(const Team& t, const Mem& M, const EpaResumeSink& sink, EpaOut& o, int nv, int fend,
+                     int it, int st, float scale2) {
+  if (!sink.buf) return;
+  int slot = -1;
+  if (t.lane() == 0) {
+#if defined(__CUDA_ARCH__)
+    slot = atomicAdd(sink.count, 1);
+#else
+    slot = (*sink.count)++;
+#endif
+  }
+  slot = t.imax(slot);
+  if (slot >= sink.cap) return;
+  EpaResume& R = sink.buf[slot];
+  for (int j = t.lane(); j < nv; j += Team::L) {
+    R.vp[j] = M.vp[j];
+    R.vid[j] = M.vid[j];
+  }
+  for (int f = t.lane(); f < fend; f += Team::L) {
+    R.fn[f] = M.fn[f];
+    for (int k = 0; k < 4; ++k) {
+      R.fv[f][k] = M.fv[f][k];
+      R.fa[f][k] = M.fa[f][k];
+    }
+  }
+  if (t.lane() == 0) {
+    R.nv = nv;
+    R.fend = fend;
+    R.it = it;
+    R.st = st;
+    R.status = o.status;
+    R.scale2 = scale2;
+  }
+  o.resume = slot;
+}
+
 // Run EPA for one pair whose GJK result is g.  `M` is this pair's shared working set.
 //
 // One expansion step, with the faces of the polytope split over the team's lanes
@@ -312,9 +371,12 @@ OGX_HD void epa_polish(const Bodies& B, EpaOut& o) {
 // The next step's closest face is the team's minimum over the candidates.
 // kCert (the full-capacity re-run only): with FP64 face planes on, run the certified
 // expansion described at kEpaCertGain.
+// sink: where a capacity spill saves itself (small pass); rs: a saved expansion to
+// continue instead of starting from the GJK simplex (full pass).
 template <bool kCert = false, class Team, class Bodies, class Mem>
 OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const GjkState& g,
-                     Mem& M, EpaOut& o, bool can_spill) {
+                     Mem& M, EpaOut& o, bool can_spill, EpaResumeSink sink = EpaResumeSink{nullptr, nullptr, 0},
+                     const EpaResume* rs = nullptr) {
   const int L = Team::L;
   const int lane = t.lane();
   const bool escalate = (cfg.flags & OGX_F_FP64_ESCALATE) != 0;
@@ -325,12 +387,45 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   o.polish = false;
   o.spill = false;
   o.spill64 = false;
+  o.resume = -1;
   o.dist = g.dist;
   o.w0 = g.w0;
   o.w1 = g.w1;
   o.nrm = unit_or_x(g.w1 - g.w0);
   if (g.n != 4 && g.dist > FLT_EPSILON) return;  // separated (EPA.c:369-373)
   o.status |= OGX_S_EPA_RUN;
+  float scale2 = 0.0f;
+  int st = 0;
+  // per-lane closest candidate (slot, plane distance); -1 = none
+  float cbd = INFINITY;
+  int cbest = -1;
+  int nv = 4, fend = 4;
+  int it = 0;
+  if (rs) {
+    nv = rs->nv;
+    fend = rs->fend;
+    it = rs->it;
+    st = rs->st;
+    scale2 = rs->scale2;
+    o.status = rs->status;
+    for (int j = lane; j < nv; j += L) {
+      M.vp[j] = rs->vp[j];
+      M.vid[j] = rs->vid[j];
+    }
+    for (int f = lane; f < fend; f += L) {
+      M.fn[f] = rs->fn[f];
+      for (int k = 0; k < 4; ++k) {
+        M.fv[f][k] = rs->fv[f][k];
+        M.fa[f][k] = rs->fa[f][k];
+      }
+    }
+    t.sync();
+    for (int f = lane; f < fend; f += L)
+      if (M.fv[f][3] && M.fn[f].w < cbd) {
+        cbd = M.fn[f].w;
+        cbest = f;
+      }
+  } else {
 
   // ---- grow the simplex to a tetrahedron (EPA.c:375-583)
   // simplex in registers: every index below is a constant after unrolling
@@ -407,7 +502,6 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   // (0, i2, i1), (0, i1, 3), (i1, i2, 3), (i2, 0, 3).  Face across edge k of face f
   // (edge k = vertices k, k+1 mod 3) is the same for both orientations.
   const int i1 = vol >= 0.0f ? 1 : 2, i2 = vol >= 0.0f ? 2 : 1;
-  float scale2 = 0.0f;
   if (lane == 0) {
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -418,10 +512,6 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
 #pragma unroll
   for (int j = 0; j < 4; ++j) scale2 = fmaxf(scale2, dot(P[j], P[j]));
   t.sync();
-  int st = 0;
-  // per-lane closest candidate (slot, plane distance); -1 = none
-  float cbd = INFINITY;
-  int cbest = -1;
   for (int f = lane; f < 4; f += L) {
     const int va = f == 2 ? i1 : (f == 3 ? i2 : 0);
     const int vb = f == 0 ? i2 : (f == 1 ? i1 : (f == 2 ? i2 : 0));
@@ -441,11 +531,10 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       cbest = f;
     }
   }
-  int nv = 4, fend = 4;
   t.sync();
+  }
 
   const float tol_floor = cfg.epa_tol;
-  int it = 0;
   int best = -1;
   bool done = false;
   while (it < cfg.epa_max_iter) {
@@ -515,6 +604,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     }
     if (nv >= Mem::kV) {
       if (can_spill) {
+        epa_save(t, M, sink, o, nv, fend, it - 1, st, scale2);
         o.spill = true;
         return;
       }
@@ -606,6 +696,7 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     }
     if (fend + (htot > nvis ? htot - nvis : 0) > Mem::kF) {
       if (can_spill) {
+        epa_save(t, M, sink, o, nv - 1, fend, it - 1, st, scale2);  // before q was added
         o.spill = true;
         return;
       }

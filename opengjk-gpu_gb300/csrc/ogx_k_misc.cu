@@ -280,7 +280,12 @@ __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B, int late) {
   cfg64.flags |= OGX_F_EPA_FP64_PLANES;
   for (int j = team; j < cnt; j += nteams) {
     const int e = late ? B.spill[B.npairs - 1 - j] : B.spill[j];
-    epa_item<32, 0, true>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
+    if (e & kSpillResume) {  // continue the small pass's saved expansion
+      const EpaResume* rs = B.resume + (e & (kSpillResume - 1));
+      epa_item<32, 0, true>(t, B, B.cfg, rs->pair, M, false, nullptr, rs);
+    } else {
+      epa_item<32, 0, true>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
+    }
     t.sync();
   }
 }

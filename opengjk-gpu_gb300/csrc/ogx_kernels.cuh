@@ -53,7 +53,8 @@ constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to conti
 constexpr int kCntSpill = 2 * kBuckets + 3;  // contacts that outgrew the small EPA capacity
 constexpr int kCntRefineBig = 2 * kBuckets + 4;  // of the FP64 continuations, bodies > 128 points
 constexpr int kCntSpillLate = 2 * kBuckets + 5;  // contacts found by the FP64 refinement
-constexpr int kCntSlots = 2 * kBuckets + 6;
+constexpr int kCntResume = 2 * kBuckets + 6;  // capacity spills saved for the full pass to resume
+constexpr int kCntSlots = 2 * kBuckets + 7;
 // FP64 continuations of pairs whose bodies have at most this many points run one thread
 // per pair (FP64 instructions then serve 32 pairs); larger ones one warp per pair
 constexpr int kRefineLaneMax = 128;
@@ -77,6 +78,8 @@ struct DevBatch {
   int* refine_full;   // npairs entries: pair ids whose FP32 support was not certain
                       // (small bodies from the front, large ones from the back)
   int* spill;         // npairs entries: contacts to re-run at full EPA capacity
+  EpaResume* resume;  // resume_cap saved small-capacity expansions (null: none)
+  int resume_cap;
   const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
   const uint32_t* subtab;  // sub-distance decision table (fill_subtab); null: the tree
   ogx_config cfg;
@@ -208,24 +211,29 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
   }
 }
 
-// spill list entries: pair index, top bit set when the re-run needs FP64 face planes
-constexpr int kSpill64 = 1 << 30;
 
 // kFull: the full-capacity pass over the spill list -- certified re-runs where the entry
 // asks for FP64 planes, and the FP64 polish of the result done here by lane 0 instead of
 // through the polish list, so that the polish pass need not wait for this one
+// spill list entry codes: a pair index, or a saved expansion to resume
+constexpr int kSpill64 = 1 << 30;      // the re-run solves every face plane in FP64
+constexpr int kSpillResume = 1 << 29;  // low bits: the EpaResume record to continue
+
 template <int L, int K, bool kFull = false, class Mem>
 __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
-                                         Mem& M, bool can_spill, bool* spill64 = nullptr) {
+                                         Mem& M, bool can_spill, int* spill_code = nullptr,
+                                         const EpaResume* rs = nullptr) {
   const int2 pr = B.pairs[p];
   typename SrcOf<L, K>::type src;
   bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
   GjkState g;
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
-  epa_pair<kFull>(t, src, cfg, g, M, o, can_spill);
+  const EpaResumeSink sink{can_spill ? B.resume : nullptr, B.counts + kCntResume, B.resume_cap};
+  epa_pair<kFull>(t, src, cfg, g, M, o, can_spill, sink, rs);
   if (o.spill) {
-    if (spill64) *spill64 = o.spill64;
+    if (o.resume >= 0 && t.lane() == 0) B.resume[o.resume].pair = p;
+    if (spill_code) *spill_code = o.resume >= 0 ? (kSpillResume | o.resume) : (p | (o.spill64 ? kSpill64 : 0));
     return false;
   }
   const bool lead = t.lane() == 0;
@@ -274,11 +282,11 @@ __global__ void __launch_bounds__(128, OCC) k_epa(DevBatch B, int bucket) {
   const int* list = B.elists + (size_t)bucket * B.npairs;
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
-    bool s64 = false;
-    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true, &s64);
+    int code = 0;
+    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true, &code);
     const bool lead = t.lane() == 0;
     const int q = warp_append(B.counts + kCntSpill, lead && !ok);
-    if (lead && !ok) B.spill[q] = p | (s64 ? kSpill64 : 0);
+    if (lead && !ok) B.spill[q] = code;
     t.sync();  // the next pair reuses M
   }
 }

@@ -171,6 +171,8 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
   B.refine_full = reinterpret_cast<int*>(S->scratch + kOffRefineFull);
   B.polish = reinterpret_cast<PolishRec*>(S->scratch + kOffPolish);
   B.spill = reinterpret_cast<int*>(S->scratch + kOffSpill);
+  B.resume = nullptr;  // capacity spills restart at full capacity
+  B.resume_cap = 0;
   B.warm = nullptr;
   B.subtab = nullptr;  // the decision tree (same outcomes as the engine's table)
   B.cfg = c;

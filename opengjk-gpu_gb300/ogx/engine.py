@@ -151,13 +151,13 @@ class Context:
         return self.kernel_choice()
 
     def work_counts(self) -> dict:
-        c = (ctypes.c_int32 * 20)()
-        n = self.lib.ogx_ctx_work_counts(self.handle, c, 20)
-        if n != 20:
+        c = (ctypes.c_int32 * 21)()
+        n = self.lib.ogx_ctx_work_counts(self.handle, c, 21)
+        if n != 21:
             raise _lib.OgxError(-2, "work counts unavailable")
         return {"gjk": list(c[0:7]), "epa": list(c[7:14]), "polish": int(c[14]), "refine": int(c[15]),
                 "refine_full": int(c[16]) + int(c[18]), "refine_full_warp": int(c[18]),
-                "epa_spill": int(c[17]), "epa_late": int(c[19])}
+                "epa_spill": int(c[17]), "epa_late": int(c[19]), "epa_resumed": min(int(c[20]), 4096)}
 
 
 class Pool:
