@@ -114,6 +114,9 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
     s = c->ensure_scratch(widest);
   }
   if (!s) s = ctx->ensure_stage(0, (size_t)pool->npoints * 3 * sizeof(float));
+  // the last range runs on this context, with every size bucket on a stream of its own:
+  // nothing else is left to overlap it with, so its latency is the tail of the call
+  if (!s && C > 1) s = ctx->ensure_scratch(widest);
   if (s) return s;
 
   // optional timeline (context timing on): per chunk, the end of its body upload, the end
@@ -170,7 +173,7 @@ ogx_status streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs, 
     if (e == cudaSuccess) e = cudaEventRecord(ev_packed[j], ctx->stream);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "streamed pack");
     launches += bb[j + 1] > bb[j];
-    ogx_ctx* c = ctx->sub[j % S];
+    ogx_ctx* c = (j == C - 1 && C > 1) ? ctx : ctx->sub[j % S];
     cudaStream_t cs = c->stream;
     e = cudaStreamWaitEvent(cs, ev_packed[j], 0);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, ev_pair[j], 0);
