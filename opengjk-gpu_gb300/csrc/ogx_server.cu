@@ -364,6 +364,9 @@ void ogx_server::loop() {
             r->out_count[1] = s.h_bres[1];
           }
           r->npairs = std::min(found, std::min(r->max_pairs, sc.slot_pairs));
+          // the narrow phase holds only the pairs found: release the rest of the budget
+          pairs_in_flight -= s.reserved - r->npairs;
+          s.reserved = r->npairs;
           failed = !launch_narrow(r, s, s.world);
         } else {
           r->err = ogx_cuda_fail(q, "server broad phase");
