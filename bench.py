@@ -219,6 +219,19 @@ def plain_form_baseline(batch, device: int, steps: int = 3) -> dict:
             "sample": "the whole workload, points resident in HBM, 1 warm-up step"}
 
 
+def latency_summary(reqs) -> dict:
+    """p50 / p99 of the requests' latencies, the median of each phase, and the mean
+    phases of the ticks at or above the p99 (what the tail is made of)."""
+    lat = np.array([r.latency_ms for r in reqs])
+    ph = np.array([r.phases_ms for r in reqs])
+    p99 = float(np.percentile(lat, 99))
+    tail = ph[lat >= min(p99, lat.max())]
+    names = ("queued", "staging", "device", "rest")
+    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99,
+            "phases_median_ms": dict(zip(names, np.round(np.median(ph, axis=0), 4).tolist())),
+            "phases_tail_ms": dict(zip(names, np.round(tail.mean(axis=0), 4).tolist()))}
+
+
 def serving_report(device: int, seed: int = 77) -> dict:
     """Serving loop on 20k resident rigid bodies (log-uniform 8-512 vertices): ticks of
     1k-200k candidate pairs (log-uniform) arrive as a Poisson process; each tick uploads
@@ -269,15 +282,15 @@ def serving_report(device: int, seed: int = 77) -> dict:
                     out[k] = srv.submit(v, lists[i])
             thr = th.Thread(target=submitter)
             thr.start()
-            lat = []
+            done = []
             for k in range(n_ticks):
                 while out[k] is None:
                     time.sleep(5e-5)
-                lat.append(srv.wait(out[k]).latency_ms)
+                done.append(srv.wait(out[k]))
             thr.join()
             span = time.perf_counter() - t0
             pairs = float(sum(sizes[int(i)] for i in order))
-            return np.array(lat), pairs / span
+            return done, pairs / span
 
         mix_rate = 0.5 * cap_pairs_s / float(sizes.mean())
         lat_mix, thr_mix = run(list(range(n_lists)), mix_rate, 300, seed + 1)
@@ -314,9 +327,8 @@ def serving_report(device: int, seed: int = 77) -> dict:
         for k in range(len(arrivals)):
             while outb[k] is None:
                 time.sleep(5e-5)
-            lat_b.append(srv.wait(outb[k]).latency_ms)
+            lat_b.append(srv.wait(outb[k]))
         thr.join()
-        lat_b = np.array(lat_b)
     finally:
         srv.close()
     return {
@@ -324,15 +336,15 @@ def serving_report(device: int, seed: int = 77) -> dict:
         "tick_pairs": "log-uniform [1k, 200k] (phase 1), 200k (phase 2)",
         "arrivals": "Poisson", "warm_start": True, "slots": 4, "max_pairs_in_flight": 600_000,
         "capacity_pairs_per_s": cap_pairs_s, "capacity_200k_ticks_per_s": cap_big_hz,
-        "mixed": {"rate_hz": mix_rate, "ticks": len(lat_mix), "pairs_per_s": thr_mix,
-                  "p50_ms": float(np.percentile(lat_mix, 50)), "p99_ms": float(np.percentile(lat_mix, 99))},
+        "mixed": {"rate_hz": mix_rate, "ticks": len(lat_mix), "pairs_per_s": thr_mix, **latency_summary(lat_mix)},
         "ticks_200k": {"rate_hz": big_rate, "ticks": len(lat_big), "pairs_per_s": thr_big,
-                       "p50_ms": float(np.percentile(lat_big, 50)), "p99_ms": float(np.percentile(lat_big, 99))},
+                       **latency_summary(lat_big)},
         "broadphase_ticks": {"rate_hz": broad_rate, "ticks": len(lat_b), "cell": cell, "margin": margin,
                              "mean_pairs_per_tick": float(np.mean(found)),
-                             "capacity_ticks_per_s": cap_broad_hz,
-                             "p50_ms": float(np.percentile(lat_b, 50)), "p99_ms": float(np.percentile(lat_b, 99))},
-        "latency": "submit -> results in host memory, host clock",
+                             "capacity_ticks_per_s": cap_broad_hz, **latency_summary(lat_b)},
+        "latency": "submit -> results in host memory, host clock; phases: queued for a slot, host "
+                   "staging, device (events around the request's work), rest (issue and completion "
+                   "detection)",
     }
 
 
