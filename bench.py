@@ -224,15 +224,20 @@ def latency_summary(reqs) -> dict:
     phases of the ticks at or above the p99 (what the tail is made of)."""
     lat = np.array([r.latency_ms for r in reqs])
     ph = np.array([r.phases_ms for r in reqs])
+    lag = np.array([r.lag_ms for r in reqs])
     p99 = float(np.percentile(lat, 99))
     tail = ph[lat >= min(p99, lat.max())]
     names = ("queued", "staging", "device", "rest")
+    sched = lat + lag
     return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": p99,
+            "from_arrival_p50_ms": float(np.percentile(sched, 50)),
+            "from_arrival_p99_ms": float(np.percentile(sched, 99)),
+            "submit_lag_p50_ms": float(np.percentile(lag, 50)), "submit_lag_max_ms": float(lag.max()),
             "phases_median_ms": dict(zip(names, np.round(np.median(ph, axis=0), 4).tolist())),
             "phases_tail_ms": dict(zip(names, np.round(tail.mean(axis=0), 4).tolist()))}
 
 
-def serving_report(device: int, seed: int = 77) -> dict:
+def serving_report(device: int, seed: int = 77, slots: int = 4, max_in_flight: int = 600_000) -> dict:
     """Serving loop on 20k resident rigid bodies (log-uniform 8-512 vertices): ticks of
     1k-200k candidate pairs (log-uniform) arrive as a Poisson process; each tick uploads
     new poses and submits its pairs; latency = submit -> results in host memory.  Phase 1
@@ -247,8 +252,8 @@ def serving_report(device: int, seed: int = 77) -> dict:
     sizes[-6:] = 200_000
     lists = [scene.candidate_pairs(t, int(n)) for t, n in enumerate(sizes)]
     xfs = [scene.transforms(t) for t in range(n_lists)]
-    srv = serving.Server(scene.counts, scene.local, device=device, slots=4, slot_pairs=262144,
-                         max_pairs_in_flight=600_000, world_slots=8, warm_start=True)
+    srv = serving.Server(scene.counts, scene.local, device=device, slots=slots, slot_pairs=262144,
+                         max_pairs_in_flight=max_in_flight, world_slots=8, warm_start=True)
     try:
         # capacity: back-to-back requests of each list, results waited in order
         def burst(idx):
@@ -258,7 +263,7 @@ def serving_report(device: int, seed: int = 77) -> dict:
                 v = srv.set_transforms(xfs[i])
                 reqs.append(srv.submit(v, lists[i]))
             for r in reqs:
-                srv.wait(r)
+                srv.wait(r).release()
             return time.perf_counter() - t0
         burst(range(n_lists))  # warm-up (and warm-start table fill)
         dt = burst(range(n_lists))
@@ -271,6 +276,7 @@ def serving_report(device: int, seed: int = 77) -> dict:
             arrivals = W.poisson_arrivals(seed2, n_ticks, rate_hz)
             order = np.random.default_rng(seed2).choice(phase_lists, size=n_ticks)
             out = [None] * n_ticks
+            lag = [0.0] * n_ticks
             t0 = time.perf_counter() + 0.05
 
             def submitter():
@@ -279,6 +285,7 @@ def serving_report(device: int, seed: int = 77) -> dict:
                         time.sleep(5e-5)
                     i = int(order[k])
                     v = srv.set_transforms(xfs[i])
+                    lag[k] = (time.perf_counter() - t0 - arrivals[k]) * 1e3
                     out[k] = srv.submit(v, lists[i])
             thr = th.Thread(target=submitter)
             thr.start()
@@ -287,9 +294,12 @@ def serving_report(device: int, seed: int = 77) -> dict:
                 while out[k] is None:
                     time.sleep(5e-5)
                 done.append(srv.wait(out[k]))
+                done[-1].release()
             thr.join()
             span = time.perf_counter() - t0
             pairs = float(sum(sizes[int(i)] for i in order))
+            for r, g in zip(done, lag):
+                r.lag_ms = g
             return done, pairs / span
 
         mix_rate = 0.5 * cap_pairs_s / float(sizes.mean())
@@ -304,23 +314,27 @@ def serving_report(device: int, seed: int = 77) -> dict:
         def broad_burst(n):
             t0 = time.perf_counter()
             reqs = [srv.submit_broadphase(srv.set_transforms(xfs[k % n_lists]), cell, margin) for k in range(n)]
+            found = []
             for r in reqs:
-                srv.wait(r)
-            return time.perf_counter() - t0, reqs
+                found.append(int(srv.wait(r).count[0]))
+                r.release()
+            return time.perf_counter() - t0, found
         broad_burst(n_lists)
-        dtb, reqs = broad_burst(n_lists)
-        found = [int(r.count[0]) for r in reqs]
+        dtb, found = broad_burst(n_lists)
         cap_broad_hz = n_lists / dtb
         broad_rate = 0.5 * cap_broad_hz
         arrivals = W.poisson_arrivals(seed + 3, 200, broad_rate)
         outb = [None] * len(arrivals)
+        lagb = [0.0] * len(arrivals)
         t0 = time.perf_counter() + 0.05
 
         def submitter_b():
             for k in range(len(arrivals)):
                 while time.perf_counter() < t0 + arrivals[k]:
                     time.sleep(5e-5)
-                outb[k] = srv.submit_broadphase(srv.set_transforms(xfs[k % n_lists]), cell, margin)
+                v = srv.set_transforms(xfs[k % n_lists])
+                lagb[k] = (time.perf_counter() - t0 - arrivals[k]) * 1e3
+                outb[k] = srv.submit_broadphase(v, cell, margin)
         thr = th.Thread(target=submitter_b)
         thr.start()
         lat_b = []
@@ -328,13 +342,15 @@ def serving_report(device: int, seed: int = 77) -> dict:
             while outb[k] is None:
                 time.sleep(5e-5)
             lat_b.append(srv.wait(outb[k]))
+            lat_b[-1].release()
+            lat_b[-1].lag_ms = lagb[k]
         thr.join()
     finally:
         srv.close()
     return {
         "bodies": scene.n_bodies, "mean_vertices": float(scene.counts.mean()),
         "tick_pairs": "log-uniform [1k, 200k] (phase 1), 200k (phase 2)",
-        "arrivals": "Poisson", "warm_start": True, "slots": 4, "max_pairs_in_flight": 600_000,
+        "arrivals": "Poisson", "warm_start": True, "slots": slots, "max_pairs_in_flight": max_in_flight,
         "capacity_pairs_per_s": cap_pairs_s, "capacity_200k_ticks_per_s": cap_big_hz,
         "mixed": {"rate_hz": mix_rate, "ticks": len(lat_mix), "pairs_per_s": thr_mix, **latency_summary(lat_mix)},
         "ticks_200k": {"rate_hz": big_rate, "ticks": len(lat_big), "pairs_per_s": thr_big,

@@ -19,7 +19,9 @@ ERRORS = {
     -3: "OGX_ERR_NOMEM",
     -4: "OGX_ERR_NO_DEVICE",
     -5: "OGX_ERR_CAPACITY",
+    -6: "OGX_ERR_BUSY",
 }
+ERR_BUSY = -6
 
 FLAG_FP64_ESCALATE = 1
 FLAG_FP64_POLISH = 2

@@ -57,27 +57,64 @@ def _pinned(nbytes: int):
     return t, t.numpy()[:nbytes]
 
 
+_SET_FIELDS = (("dist", np.float32, ()), ("simplex", None, ()), ("normal", np.float32, (3,)),
+               ("status", np.int32, ()), ("pairs", np.int32, (2,)))
+
+
+class _ResultSets:
+    """Page-locked result arrays for requests of up to `cap` pairs, kept and handed out
+    again when a request is released, so that a running server allocates no pinned
+    memory per request (pinning tens of MB takes milliseconds)."""
+
+    def __init__(self, cap: int):
+        self.cap = cap
+        self.free = []
+
+    def new(self, n: int) -> dict:
+        out = {}
+        for name, dtype, tail in _SET_FIELDS:
+            dt = np.dtype(_lib.SIMPLEX_DTYPE if dtype is None else dtype)
+            shape = (n,) + tail
+            t, raw = _pinned(int(np.prod(shape)) * dt.itemsize)
+            out[name] = (t, raw.view(dt).reshape(shape))
+        t, raw = _pinned(8)
+        out["count"] = (t, raw.view(np.int32))
+        return out
+
+    def take(self, n: int) -> tuple[dict, bool]:
+        if n > self.cap:
+            return self.new(n), False
+        return (self.free.pop() if self.free else self.new(self.cap)), True
+
+
 class Request:
     """Host result arrays of one submitted request (filled when it completes).  They are
-    page-locked, so the device writes them directly."""
+    page-locked, so the device writes them directly.  ``release()`` hands them back to
+    the server for later requests; without it they are freed with the request."""
 
-    def __init__(self, ticket: int, pairs: np.ndarray, n: int):
+    def __init__(self, ticket: int, pairs: np.ndarray | None, n: int, bufs: dict, pool: _ResultSets | None):
         self.ticket = ticket
+        self._set = bufs
+        self._pool = pool
+        self.dist = bufs["dist"][1][:n]
+        self.simplex = bufs["simplex"][1][:n]
+        self.normal = bufs["normal"][1][:n]
+        self.status = bufs["status"][1][:n]
         self.pairs = pairs
-        self._bufs = []
-
-        def arr(dtype, shape):
-            dt = np.dtype(dtype)
-            t, raw = _pinned(int(np.prod(shape)) * dt.itemsize)
-            self._bufs.append(t)
-            return raw.view(dt).reshape(shape)
-        self.dist = arr(np.float32, (n,))
-        self.simplex = arr(_lib.SIMPLEX_DTYPE, (n,))
-        self.normal = arr(np.float32, (n, 3))
-        self.status = arr(np.int32, (n,))
         self.latency_ms = None
         self.phases_ms = None
         self.count = None  # broad-phase requests: [pairs found, error flags]
+        self.done = False
+
+    def release(self):
+        """Give the result arrays back to the server (after wait()); the request's arrays,
+        and any view of them, must not be used afterwards."""
+        if not self.done:
+            raise RuntimeError("release() before the request was waited for")
+        if self._pool is not None and self._set is not None:
+            self._pool.free.append(self._set)
+        self._set = None
+        self.dist = self.simplex = self.normal = self.status = self.pairs = self.count = None
 
     def results(self) -> dict:
         n = self.n_run
@@ -95,7 +132,9 @@ class Request:
 class Server:
     def __init__(self, counts, local_xyz, config: _lib.Config | None = None, device: int = 0, slots: int = 4,
                  slot_pairs: int = 262144, max_pairs_in_flight: int = 1 << 20, world_slots: int = 4,
-                 warm_start: bool = True, warm_capacity_log2: int = 22):
+                 warm_start: bool = True, warm_capacity_log2: int = 22, result_sets: int | None = None):
+        """`result_sets` page-locked result sets of `slot_pairs` pairs are allocated up
+        front (default 2 x slots) and recycled by Request.release()."""
         self.lib = _lib.load()
         _bind(self.lib)
         sc = ServerConfig()
@@ -111,6 +150,9 @@ class Server:
         _lib.check(rc)
         self.handle = h
         self._live = {}
+        self._sets = _ResultSets(slot_pairs)
+        for _ in range(2 * slots if result_sets is None else result_sets):
+            self._sets.free.append(self._sets.new(slot_pairs))
 
     def set_transforms(self, xf: np.ndarray) -> int:
         xf = np.ascontiguousarray(xf, np.float32)
@@ -123,7 +165,8 @@ class Server:
         pairs = np.ascontiguousarray(pairs, np.int32)
         n = int(pairs.shape[0])
         t = ctypes.c_int64()
-        req = Request(0, pairs, n)
+        bufs, pooled = self._sets.take(n)
+        req = Request(0, pairs, n, bufs, self._sets if pooled else None)
         _lib.check(self.lib.ogx_server_submit(self.handle, int(version), n, pairs.ctypes.data,
                                               req.simplex.ctypes.data, req.dist.ctypes.data,
                                               req.normal.ctypes.data, req.status.ctypes.data, ctypes.byref(t)))
@@ -136,12 +179,10 @@ class Server:
         `margin` that overlap), then GJK + EPA on them.  req.pairs[:req.n_run] are the
         pairs run, req.count[0] the number found."""
         t = ctypes.c_int64()
-        req = Request(0, None, max_pairs)
-        pb, pairs = _pinned(max_pairs * 8)
-        cb, cnt = _pinned(8)
-        req._bufs += [pb, cb]
-        req.pairs = pairs.view(np.int32).reshape(max_pairs, 2)
-        req.count = cnt.view(np.int32)
+        bufs, pooled = self._sets.take(max_pairs)
+        req = Request(0, None, max_pairs, bufs, self._sets if pooled else None)
+        req.pairs = bufs["pairs"][1][:max_pairs]
+        req.count = bufs["count"][1]
         _lib.check(self.lib.ogx_server_submit_broadphase(
             self.handle, int(version), float(cell), float(margin), int(max_pairs), req.pairs.ctypes.data,
             req.count.ctypes.data, req.simplex.ctypes.data, req.dist.ctypes.data, req.normal.ctypes.data,
@@ -161,7 +202,11 @@ class Server:
         lat = ctypes.c_double()
         ph = (ctypes.c_double * 4)()
         rc = self.lib.ogx_server_wait_phases(self.handle, req.ticket, float(timeout_s), ctypes.byref(lat), ph)
-        self._live.pop(req.ticket, None)
+        if rc != _lib.ERR_BUSY:
+            # done or failed: the device no longer writes the arrays (a timed-out request
+            # stays registered, its arrays alive)
+            self._live.pop(req.ticket, None)
+            req.done = True
         _lib.check(rc)
         req.latency_ms = lat.value
         req.phases_ms = tuple(ph)

@@ -156,3 +156,29 @@ def test_latency_phases(scene):
             assert rest > -0.05, req.phases_ms
             assert abs(q + stg + dev + rest - req.latency_ms) < 1e-6
             assert dev <= req.latency_ms + 0.05
+
+
+def test_result_sets_recycled(scene, engine):
+    """A released request's page-locked arrays serve the next request (no pinned
+    allocation per request), and its results are still exact; release() before the
+    request was waited for is refused."""
+    xf = scene.transforms(9)
+    with _server(scene, warm_start=False, slots=2, result_sets=1) as srv:
+        v = srv.set_transforms(xf)
+        first = srv.submit(v, scene.candidate_pairs(9, 3000))
+        with pytest.raises(RuntimeError):
+            first.release()
+        srv.wait(first)
+        addr = first.dist.ctypes.data
+        first.release()
+        assert first.dist is None
+        pairs = scene.candidate_pairs(9, 5000)
+        second = srv.wait(srv.submit(v, pairs))
+        assert second.dist.ctypes.data == addr
+        ref = engine.query(_batch(scene, scene.world(xf), pairs), engine.MODE_GJK_EPA)
+        assert np.array_equal(second.dist, ref["dist"])
+        assert np.array_equal(second.simplex["witnesses"], ref["simplex"]["witnesses"])
+        # while the one set is held by an unreleased request, the next one gets a new set
+        third = srv.submit(v, scene.candidate_pairs(9, 3000))
+        assert third.dist.ctypes.data != addr
+        srv.wait(third)
