@@ -84,7 +84,10 @@ class _ResultSets:
     def take(self, n: int) -> tuple[dict, bool]:
         if n > self.cap:
             return self.new(n), False
-        return (self.free.pop() if self.free else self.new(self.cap)), True
+        try:  # list.pop is atomic: submit and release may run on different threads
+            return self.free.pop(), True
+        except IndexError:
+            return self.new(self.cap), True
 
 
 class Request:
