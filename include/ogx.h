@@ -341,7 +341,9 @@ ogx_status ogx_server_destroy(ogx_server* server);
 /* New poses: xf[num_bodies][12] = row-major rotation R (9) then translation t (3); the
  * world point is R p + t evaluated in double and rounded once to float.  Returns the
  * version to submit requests against.  Blocks (at most 10 s, then OGX_ERR_BUSY) while
- * the ring slot it overwrites is still used by a queued or running request. */
+ * the ring slot it overwrites is still used by a queued or running request.  Several
+ * threads may call it at once (each gets its own version); the copy and the upload run
+ * without holding the server's lock, so requests keep being admitted meanwhile. */
 ogx_status ogx_server_set_transforms(ogx_server* server, const float* xf, int64_t* version);
 /* Queue a request: npairs <= slot_pairs pairs of body indices (copied at once); the
  * results are written to the host arrays (any of them may be NULL) before the request

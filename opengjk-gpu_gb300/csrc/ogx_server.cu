@@ -199,6 +199,7 @@ struct ogx_server {
   std::vector<float*> h_xf;
   std::vector<int64_t> world_version;
   std::vector<int> world_refs;
+  std::vector<char> world_writing;  // a transform upload into the slot is under way
   std::vector<cudaEvent_t> world_ready;
   int64_t next_version = 0;
   std::vector<Slot> slots;
@@ -536,6 +537,7 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
     S->world_ready.push_back(ev);
     S->world_version.push_back(-1);
     S->world_refs.push_back(0);
+    S->world_writing.push_back(0);
   }
   // Slots spread their size buckets over streams of their own only as far as the
   // process's hardware work queues go (CUDA_DEVICE_MAX_CONNECTIONS, 8 by default): a
@@ -610,20 +612,34 @@ extern "C" ogx_status ogx_server_destroy(ogx_server* S) {
 extern "C" ogx_status ogx_server_set_transforms(ogx_server* S, const float* xf, int64_t* version) {
   if (!S || !xf || !version) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
   std::unique_lock<std::mutex> lk(S->mu);
-  const int64_t v = S->next_version;
-  const int w = (int)(v % S->sc.world_slots);
-  // the ring slot must not be read by a request in flight or queued
-  auto in_use = [&] {
-    if (S->world_refs[w] > 0) return true;
+  // the next version's ring slot must not be read by a request in flight or queued, nor
+  // be written by another upload (another caller may take that version meanwhile)
+  auto in_use = [&](int w) {
+    if (S->world_refs[w] > 0 || S->world_writing[w]) return true;
     for (Request* r : S->queue)
       if (r->version % S->sc.world_slots == w && r->version == S->world_version[w]) return true;
     return false;
   };
   const auto deadline = Clock::now() + std::chrono::seconds(10);
-  while (in_use()) {
-    if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && in_use())
-      return ogx_fail(OGX_ERR_BUSY, "transform ring slot %d still in use after 10 s", w);
+  int64_t v_mine = S->next_version;
+  int w = (int)(v_mine % S->sc.world_slots);
+  while (in_use(w)) {
+    if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout) {
+      v_mine = S->next_version;
+      w = (int)(v_mine % S->sc.world_slots);
+      if (in_use(w)) return ogx_fail(OGX_ERR_BUSY, "transform ring slot %d still in use after 10 s", w);
+      break;
+    }
+    v_mine = S->next_version;
+    w = (int)(v_mine % S->sc.world_slots);
   }
+  // reserve the version and the slot, then stage and upload without the lock: the
+  // scheduler keeps admitting and completing requests meanwhile (the copy into the pinned
+  // staging alone takes ~0.3 ms for 20k bodies)
+  S->next_version = v_mine + 1;
+  S->world_version[w] = -1;
+  S->world_writing[w] = 1;
+  lk.unlock();
   cudaSetDevice(S->device);
   const size_t bytes = 12 * (size_t)S->local->nbodies * sizeof(float);
   // the pinned staging of this ring slot was last read by its previous transform upload
@@ -638,10 +654,13 @@ extern "C" ogx_status ogx_server_set_transforms(ogx_server* S, const float* xf, 
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaEventRecord(S->world_ready[w], S->pctx->stream);
+  lk.lock();
+  S->world_writing[w] = 0;
+  if (e == cudaSuccess) S->world_version[w] = v_mine;
+  lk.unlock();
+  S->cv_done.notify_all();
   if (e != cudaSuccess) return ogx_cuda_fail(e, "server transform");
-  S->world_version[w] = v;
-  S->next_version = v + 1;
-  *version = v;
+  *version = v_mine;
   return OGX_OK;
 }
 

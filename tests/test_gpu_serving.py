@@ -182,3 +182,20 @@ def test_result_sets_recycled(scene, engine):
         third = srv.submit(v, scene.candidate_pairs(9, 3000))
         assert third.dist.ctypes.data != addr
         srv.wait(third)
+
+
+def test_concurrent_transform_uploads(scene, engine):
+    """Pose uploads from several threads at once each get their own version, and each of
+    the resident versions holds exactly its own poses."""
+    from concurrent.futures import ThreadPoolExecutor
+    ticks = [11, 12, 13, 14, 15, 16]
+    pairs = scene.candidate_pairs(16, 2000)
+    with _server(scene, warm_start=False, world_slots=4) as srv:
+        with ThreadPoolExecutor(3) as ex:
+            vers = dict(ex.map(lambda t: (t, srv.set_transforms(scene.transforms(t))), ticks))
+        assert sorted(vers.values()) == list(range(min(vers.values()), min(vers.values()) + len(ticks)))
+        resident = sorted(vers, key=vers.get)[-4:]
+        for t in resident:
+            req = srv.wait(srv.submit(vers[t], pairs))
+            ref = engine.query(_batch(scene, scene.world(scene.transforms(t)), pairs), engine.MODE_GJK_EPA)
+            assert np.array_equal(req.dist, ref["dist"]), t
