@@ -80,6 +80,78 @@ def dist_env():
     return rank, world, local
 
 
+class NvmlClockSampler:
+    """SM clock, its maximum, power and clock-event reasons read through NVML every
+    `period_s` during the timed region (read-only queries; the timed region of a default
+    run lasts ~0.1 s, too short for nvidia-smi's sampling period)."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, gpu: int, period_s: float = 0.002):
+        import ctypes
+        self.ct = ctypes
+        self.period = period_s
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.nv = nv
+        self.dev = ctypes.c_void_p()
+        ok = False
+        try:  # the NVML device of this CUDA device, by UUID (NVML and CUDA numbering can differ)
+            import torch
+            uuid = str(torch.cuda.get_device_properties(gpu).uuid)
+            ok = nv.nvmlDeviceGetHandleByUUID(("GPU-" + uuid).encode(), ctypes.byref(self.dev)) == 0
+        except Exception:
+            ok = False
+        if not ok and nv.nvmlDeviceGetHandleByIndex_v2(gpu, ctypes.byref(self.dev)) != 0:
+            raise RuntimeError("no NVML handle")
+        self._reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ctypes.c_uint()
+        nv.nvmlDeviceGetMaxClockInfo(self.dev, 1, ctypes.byref(mx))
+        self.max_mhz = float(mx.value)
+
+    def _run(self):
+        c = self.ct
+        mhz, mw, r = c.c_uint(), c.c_uint(), c.c_ulonglong()
+        while not self._stop.is_set():
+            if self.nv.nvmlDeviceGetClockInfo(self.dev, 1, c.byref(mhz)) == 0:
+                self.nv.nvmlDeviceGetPowerUsage(self.dev, c.byref(mw))
+                self._reasons(self.dev, c.byref(r))
+                self.samples.append((float(mhz.value), mw.value / 1e3, int(r.value)))
+            self._stop.wait(self.period)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=5)
+        self.nv.nvmlShutdown()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0}
+        sm = [s[0] for s in self.samples]
+        reasons = sorted({name for s in self.samples for bit, name in self.REASONS.items() if s[2] & bit})
+        return {"sm_mhz": statistics.median(sm), "sm_min_mhz": min(sm), "sm_max_mhz": self.max_mhz,
+                "power_w_median": statistics.median(s[1] for s in self.samples), "reasons": reasons,
+                "samples": len(self.samples), "source": f"NVML every {self.period * 1e3:.0f} ms"}
+
+
+def clock_sampler(gpu: int):
+    """NVML sampler, or nvidia-smi's where NVML cannot be loaded."""
+    try:
+        return NvmlClockSampler(gpu)
+    except Exception:
+        return ClockSampler(gpu)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
@@ -133,6 +205,50 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def bench_config(spec: dict, n: int, batch, world: int) -> dict:
+    """The workload, identical in both arms' lines."""
+    return {"workload": spec["desc"], "pairs_per_gpu": n, "seed": 1000,
+            "mean_vertices_per_body": round(float(batch.counts.mean()), 4),
+            "l2": "inputs (pool %.2f GB) larger than L2, no flush" % (batch.coords.nbytes / 1e9),
+            "parallelism": f"replicas x{world}"}
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_single_thread(batch, seconds: float = 3.0) -> dict:
+    """The reference's own CPU loop as it ships: one thread, pair after pair, GJK then EPA
+    (examples/cpu/example.cpp:13-40), on the first pairs of the workload for ~`seconds`."""
+    from oracle import orc
+    use_ref = orc.ref_available()
+    n0 = min(batch.n_pairs, 500)
+    t = time.perf_counter()
+    _cpu_run(orc, batch.subset(np.arange(n0)), orc.MODE_GJK_EPA, 1, use_ref)
+    per_pair = max((time.perf_counter() - t) / n0, 1e-9)
+    n = int(min(batch.n_pairs, max(n0, seconds / per_pair)))
+    t = time.perf_counter()
+    _cpu_run(orc, batch.subset(np.arange(n)), orc.MODE_GJK_EPA, 1, use_ref)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": "pairs/s", "cores": 1, "kind": "reference" if use_ref else "port",
+            "sample": f"first {n} pairs of the workload, one thread, FP32 reference tolerances, {dt:.1f} s"}
+
+
 def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
     """Reference CPU GJK+EPA on the host cores (all threads), on a bounded sample of the
     same workload: the reference's own CPU build when present, else the oracle port."""
@@ -161,7 +277,8 @@ def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
             break
     return {"value": passes * n / dt, "unit": "pairs/s", "cores": threads,
             "kind": kind, "sample": f"first {n} pairs of the workload x {passes} passes, FP32 reference "
-                                   f"tolerances, {threads} threads, {dt:.1f} s ({dt * threads:.0f} core-s)"}
+                                   f"tolerances, {threads} threads, {dt:.1f} s ({dt * threads:.0f} core-s)",
+            "cpu_model": cpu_model(), "cores_1": cpu_single_thread(batch)}
 
 
 def plain_form_baseline(batch, device: int, steps: int = 3) -> dict:
@@ -224,6 +341,29 @@ def plain_form_baseline(batch, device: int, steps: int = 3) -> dict:
                       "shipped launch shapes (GJK: 256-thread blocks, 8 threads per pair; EPA: 4 pairs of "
                       "32 threads per block, 39,264 B shared memory)",
             "sample": "the whole workload, points resident in HBM, 1 warm-up step"}
+
+
+def dropin_e2e(batch, calls: int = 3) -> dict:
+    """End to end through the reference-named drop-in call compute_gjk_epa_indexed
+    (GJK/gpu/openGJK.h:497): host gkPolytope descriptors and pairs in, host simplices,
+    distances and normals out, in pageable host memory as a reference caller holds them;
+    host clock, median of `calls` calls after one warm-up call."""
+    from ogx import refapi
+    pool = refapi.Polytopes(batch.coords, batch.counts, batch.offsets)
+    pairs = np.ascontiguousarray(batch.pairs, np.int32)
+    refapi.compute_gjk_epa_indexed(pool, pairs)
+    times = []
+    for _ in range(calls):
+        t = time.perf_counter()
+        refapi.compute_gjk_epa_indexed(pool, pairs)
+        times.append(time.perf_counter() - t)
+    ms = 1e3 * statistics.median(times)
+    return {"value": batch.n_pairs / (ms / 1e3), "unit": "pairs/s", "ms_per_call": ms,
+            "calls": calls, "call_ms": [round(1e3 * t, 2) for t in times],
+            "h2d_bytes_per_step": int(batch.coords.nbytes + pairs.nbytes),
+            "d2h_bytes_per_step": int(batch.n_pairs * (108 + 4 + 12)),
+            "path": "compute_gjk_epa_indexed (reference-named C++ entry; ogx_compute_gjk_epa_indexed), "
+                    "pageable host arrays, host clock"}
 
 
 def latency_summary(reqs) -> dict:
@@ -396,6 +536,7 @@ def _cpu_run(orc, b, mode, threads, use_ref):
 
 def run_reference_arm(args):
     rank, world, _ = dist_env()
+    world = max(world, args.gpus)
     if rank != 0:
         return
     spec = WORKLOADS[args.workload]
@@ -426,10 +567,11 @@ def run_reference_arm(args):
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": spec["desc"], "pairs_per_step": ns, "sample_of": n},
+        "config": bench_config(spec, n, batch, world),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": kind,
-                         "sample": f"first {ns} of {n} pairs per step, {threads} host threads"},
+                         "sample": f"first {ns} of {n} pairs per step, {threads} host threads",
+                         "cpu_model": cpu_model(), "cores_1": cpu_single_thread(batch)},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -489,7 +631,7 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
+    with clock_sampler(local) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
         with torch.cuda.stream(stream):
@@ -608,10 +750,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": spec["desc"], "pairs_per_gpu": n, "mean_vertices_per_body":
-                   float(batch.counts.mean()), "l2": "inputs (pool %.2f GB) larger than L2, no flush"
-                   % (batch.coords.nbytes / 1e9), "parallelism": f"replicas x{world}",
-                   "launch": f"one CUDA graph per step ({launches_per_step} kernels)"},
+        "config": bench_config(spec, n, batch, world),
+        "launch": f"one CUDA graph per step ({launches_per_step} kernels)",
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
         "roofline": roof,
@@ -622,6 +762,19 @@ def run_ours(args):
     }
     if e2e:
         line["e2e"] = e2e
+        if world == 1:
+            line["dropin_e2e"] = dropin_e2e(batch)
+    parity_rep = os.path.join(ROOT, "profiles", "parity_powerlaw_1M.json")
+    if args.workload == "powerlaw" and n == 1_000_000 and os.path.exists(parity_rep):
+        # the parity report of this workload (seed 1000) from the full-size GPU test
+        # (tests/test_gpu_fullsize.py): every pair against the FP64 oracle
+        with open(parity_rep) as f:
+            rep = json.load(f)["report"]
+        line["parity"] = {k: rep[k] for k in (
+            "pairs", "in_band", "verdict_mismatch", "sep_rel_max", "sep_rel_violations", "sep_normal_err_max",
+            "sep_normal_violations", "contacts", "depth_err_max", "depth_violations", "oracle_suboptimal",
+            "normal_err_max", "normal_equivalent", "normal_violations") if k in rep}
+        line["parity"]["source"] = "profiles/parity_powerlaw_1M.json (tests/test_gpu_fullsize.py, same batch)"
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(batch)
     if not args.no_plain and world == 1:

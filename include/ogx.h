@@ -129,14 +129,14 @@ ogx_status ogx_pool_device_layout(const ogx_pool* pool, float** d_points, void**
 /* GJK over npairs pairs of pool indices (device buffers, asynchronous).
  * d_status may be NULL. */
 ogx_status ogx_gjk(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkCollisionPair* d_pairs,
-                   gkSimplex* d_simplices, float* d_distances, int32_t* d_status);
+                   ogx_simplex_f32* d_simplices, float* d_distances, int32_t* d_status);
 /* GJK then EPA on the pairs in contact (fused pipeline; d_normals n*3 floats). */
 ogx_status ogx_gjk_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
-                       const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                       const gkCollisionPair* d_pairs, ogx_simplex_f32* d_simplices,
                        float* d_distances, float* d_normals, int32_t* d_status);
 /* EPA only, from simplices and distances of an earlier GJK (in/out). */
 ogx_status ogx_epa(ogx_ctx* ctx, const ogx_pool* pool, int npairs, const gkCollisionPair* d_pairs,
-                   gkSimplex* d_simplices, float* d_distances, float* d_normals,
+                   ogx_simplex_f32* d_simplices, float* d_distances, float* d_normals,
                    int32_t* d_status);
 
 /* Kernels launched by the last engine call on this context (for accounting). */
@@ -205,7 +205,7 @@ ogx_status ogx_broad_destroy(ogx_broad* broad);
  * every result is in the host arrays (status may be NULL).  Page-locked host arrays
  * let the copies run beside the kernels.  Leaves the pool loaded with xyz. */
 ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
-                                const gkCollisionPair* pairs, gkSimplex* simplices,
+                                const gkCollisionPair* pairs, ogx_simplex_f32* simplices,
                                 float* distances, float* normals, int32_t* status, int chunks);
 
 /* ogx_gjk_epa_streamed with the caller's pieces: pair range j is
@@ -216,7 +216,7 @@ ogx_status ogx_gjk_epa_streamed(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, 
  * start computing early.  ogx_gjk_epa_streamed(..., chunks) is this call with
  * `chunks` equal ranges. */
 ogx_status ogx_gjk_epa_streamed_ranges(ogx_ctx* ctx, ogx_pool* pool, const float* xyz, int npairs,
-                                       const gkCollisionPair* pairs, gkSimplex* simplices,
+                                       const gkCollisionPair* pairs, ogx_simplex_f32* simplices,
                                        float* distances, float* normals, int32_t* status,
                                        const int* pair_bounds, int nranges, int lanes);
 
@@ -268,7 +268,7 @@ void ogx_response_params_default(ogx_response_params* params);
 ogx_status ogx_contact_response(ogx_ctx* ctx, int num_bodies, const ogx_body_state* state,
                                 int npairs, const gkCollisionPair* d_pairs,
                                 const float* d_distances, const float* d_normals,
-                                const gkSimplex* d_simplices, const ogx_response_params* params,
+                                const ogx_simplex_f32* d_simplices, const ogx_response_params* params,
                                 float* d_vel_out, float* d_ang_out, float* d_pos_out);
 
 /* Timeline of the last ogx_gjk_epa_streamed call made with timing on
@@ -285,7 +285,7 @@ int ogx_ctx_stream_timeline(const ogx_ctx* ctx, float* ms, int cap);
  * non-legacy one.  A graph must be destroyed before its context. */
 typedef struct ogx_graph ogx_graph;
 ogx_status ogx_graph_create(ogx_ctx* ctx, const ogx_pool* pool, int npairs,
-                            const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+                            const gkCollisionPair* d_pairs, ogx_simplex_f32* d_simplices,
                             float* d_distances, float* d_normals, int32_t* d_status, int mode,
                             ogx_graph** out);
 ogx_status ogx_graph_launch(ogx_graph* graph);
@@ -307,7 +307,7 @@ ogx_status ogx_graph_destroy(ogx_graph* graph);
  * stream capture.  cfg NULL = defaults; stream = cudaStream_t (NULL: legacy stream). */
 ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_bodies, int num_bodies,
                                int npairs, const gkCollisionPair* d_pairs,
-                               gkSimplex* d_simplices, float* d_distances, float* d_normals,
+                               ogx_simplex_f32* d_simplices, float* d_distances, float* d_normals,
                                int32_t* d_status, const ogx_config* cfg, void* stream);
 
 /* ------------------------------------------------------------------------- */
@@ -343,7 +343,13 @@ ogx_status ogx_server_destroy(ogx_server* server);
  * version to submit requests against.  Blocks (at most 10 s, then OGX_ERR_BUSY) while
  * the ring slot it overwrites is still used by a queued or running request.  Several
  * threads may call it at once (each gets its own version); the copy and the upload run
- * without holding the server's lock, so requests keep being admitted meanwhile. */
+ * without holding the server's lock, so requests keep being admitted meanwhile.  A
+ * version becomes valid only when its own call returns: versions handed to concurrent
+ * callers are reserved in order but may become valid out of order, and a submit against
+ * a version whose call has not returned yet is refused as not resident.  Once
+ * ogx_server_destroy has begun, new calls are refused; destroy waits for uploads
+ * already under way (at most 10 s, then OGX_ERR_BUSY with the server stopped, not
+ * freed: call destroy again). */
 ogx_status ogx_server_set_transforms(ogx_server* server, const float* xf, int64_t* version);
 /* Queue a request: npairs <= slot_pairs pairs of body indices (copied at once); the
  * results are written to the host arrays (any of them may be NULL) before the request
@@ -351,7 +357,7 @@ ogx_status ogx_server_set_transforms(ogx_server* server, const float* xf, int64_
  * (cudaMallocHost, cudaHostRegister) receive the results directly from the device;
  * others through the server's pinned staging and one host copy. */
 ogx_status ogx_server_submit(ogx_server* server, int64_t version, int npairs,
-                             const gkCollisionPair* pairs, gkSimplex* simplices,
+                             const gkCollisionPair* pairs, ogx_simplex_f32* simplices,
                              float* distances, float* normals, int32_t* status, int64_t* ticket);
 /* Queue a broad-phase request: the pairs are every pair of bodies whose boxes (grown by
  * margin) overlap in the version's world copy (ogx_broadphase on the device), then
@@ -360,7 +366,7 @@ ogx_status ogx_server_submit(ogx_server* server, int64_t version, int npairs,
  * min(count, max_pairs, slot_pairs) are run), count[1] the broad phase's error flags. */
 ogx_status ogx_server_submit_broadphase(ogx_server* server, int64_t version, float cell,
                                         float margin, int max_pairs, gkCollisionPair* pairs,
-                                        int32_t* count, gkSimplex* simplices, float* distances,
+                                        int32_t* count, ogx_simplex_f32* simplices, float* distances,
                                         float* normals, int32_t* status, int64_t* ticket);
 ogx_status ogx_server_poll(ogx_server* server, int64_t ticket, int* done);
 /* Wait for a request (timeout_s <= 0: no limit); latency_ms = completion - submission
@@ -385,46 +391,46 @@ ogx_status ogx_server_world_layout(ogx_server* server, int64_t version, float** 
 
 /* compute_minimum_distance (GJK/gpu/openGJK.h:91), GJK::GPU::computeDistances
  * (examples/gpu/example.h:21-25): GJK on pairs (bd1[i], bd2[i]), host buffers. */
-ogx_status ogx_compute_minimum_distance(int n, const gkPolytope* bd1, const gkPolytope* bd2,
-                                        gkSimplex* simplices, float* distances);
+ogx_status ogx_compute_minimum_distance(int n, const ogx_polytope_f32* bd1, const ogx_polytope_f32* bd2,
+                                        ogx_simplex_f32* simplices, float* distances);
 /* computeCollisionInformation(n, ...) (GJK/gpu/openGJK.h:112), GJK::GPU::computeEPA
  * (examples/gpu/example.h:41-46): EPA from GJK simplices/distances (in/out);
  * contact_normals (n*3) may be NULL. */
-ogx_status ogx_compute_collision_information(int n, const gkPolytope* bd1, const gkPolytope* bd2,
-                                             gkSimplex* simplices, float* distances,
+ogx_status ogx_compute_collision_information(int n, const ogx_polytope_f32* bd1, const ogx_polytope_f32* bd2,
+                                             ogx_simplex_f32* simplices, float* distances,
                                              float* contact_normals);
 /* compute_gjk_epa (GJK/gpu/openGJK.h:134), GJK::GPU::computeGJKAndEPA
  * (examples/gpu/example.h:62-67). */
-ogx_status ogx_compute_gjk_epa(int n, const gkPolytope* bd1, const gkPolytope* bd2,
-                               gkSimplex* simplices, float* distances, float* contact_normals);
+ogx_status ogx_compute_gjk_epa(int n, const ogx_polytope_f32* bd1, const ogx_polytope_f32* bd2,
+                               ogx_simplex_f32* simplices, float* distances, float* contact_normals);
 /* GJK::GPU::computeCollisionInformation as documented in README.md:39-46 (absent from
  * the reference's code): EPA with witnesses also as n*3 arrays, normals nullable. */
-ogx_status ogx_compute_collision_information_witnesses(int n, const gkPolytope* bd1,
-                                                       const gkPolytope* bd2, gkSimplex* simplices,
+ogx_status ogx_compute_collision_information_witnesses(int n, const ogx_polytope_f32* bd1,
+                                                       const ogx_polytope_f32* bd2, ogx_simplex_f32* simplices,
                                                        float* distances, float* witness1,
                                                        float* witness2, float* contact_normals);
 
 /* mid-level: allocate_and_copy_device_arrays (GJK/gpu/openGJK.h:212) */
-ogx_status ogx_allocate_and_copy_device_arrays(int n, const gkPolytope* bd1, const gkPolytope* bd2,
-                                               gkPolytope** d_bd1, gkPolytope** d_bd2,
+ogx_status ogx_allocate_and_copy_device_arrays(int n, const ogx_polytope_f32* bd1, const ogx_polytope_f32* bd2,
+                                               ogx_polytope_f32** d_bd1, ogx_polytope_f32** d_bd2,
                                                float** d_coord1, float** d_coord2,
-                                               gkSimplex** d_simplices, float** d_distances);
+                                               ogx_simplex_f32** d_simplices, float** d_distances);
 /* compute_minimum_distance_device (GJK/gpu/openGJK.h:237): descriptors and coordinates
  * in device memory */
-ogx_status ogx_compute_minimum_distance_device(int n, const gkPolytope* d_bd1,
-                                               const gkPolytope* d_bd2, gkSimplex* d_simplices,
+ogx_status ogx_compute_minimum_distance_device(int n, const ogx_polytope_f32* d_bd1,
+                                               const ogx_polytope_f32* d_bd2, ogx_simplex_f32* d_simplices,
                                                float* d_distances);
 /* compute_epa_device (GJK/gpu/openGJK.h:255) */
-ogx_status ogx_compute_epa_device(int n, const gkPolytope* d_bd1, const gkPolytope* d_bd2,
-                                  gkSimplex* d_simplices, float* d_distances,
+ogx_status ogx_compute_epa_device(int n, const ogx_polytope_f32* d_bd1, const ogx_polytope_f32* d_bd2,
+                                  ogx_simplex_f32* d_simplices, float* d_distances,
                                   float* d_contact_normals);
 /* copy_results_from_device (GJK/gpu/openGJK.h:273) */
-ogx_status ogx_copy_results_from_device(int n, const gkSimplex* d_simplices,
-                                        const float* d_distances, gkSimplex* simplices,
+ogx_status ogx_copy_results_from_device(int n, const ogx_simplex_f32* d_simplices,
+                                        const float* d_distances, ogx_simplex_f32* simplices,
                                         float* distances);
 /* free_device_arrays (GJK/gpu/openGJK.h:292) */
-ogx_status ogx_free_device_arrays(gkPolytope* d_bd1, gkPolytope* d_bd2, float* d_coord1,
-                                  float* d_coord2, gkSimplex* d_simplices, float* d_distances);
+ogx_status ogx_free_device_arrays(ogx_polytope_f32* d_bd1, ogx_polytope_f32* d_bd2, float* d_coord1,
+                                  float* d_coord2, ogx_simplex_f32* d_simplices, float* d_distances);
 /* allocate_epa_device_arrays (GJK/gpu/openGJK.h:155) */
 ogx_status ogx_allocate_epa_device_arrays(int n, float** d_witness1, float** d_witness2,
                                           float** d_contact_normals);
@@ -439,42 +445,80 @@ ogx_status ogx_free_epa_device_arrays(float* d_witness1, float* d_witness2,
 
 /* indexed: allocate_indexed_device (GJK/gpu/openGJK.h:330) */
 ogx_status ogx_allocate_indexed_device(int num_polytopes, int max_pairs,
-                                       const gkPolytope* polytopes, gkPolytope** d_polytopes,
+                                       const ogx_polytope_f32* polytopes, ogx_polytope_f32** d_polytopes,
                                        float** d_coords, gkCollisionPair** d_pairs,
-                                       gkSimplex** d_simplices, float** d_distances,
+                                       ogx_simplex_f32** d_simplices, float** d_distances,
                                        float** d_contact_normals);
 /* free_indexed_device (GJK/gpu/openGJK.h:352) */
-ogx_status ogx_free_indexed_device(gkPolytope* d_polytopes, float* d_coords,
-                                   gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+ogx_status ogx_free_indexed_device(ogx_polytope_f32* d_polytopes, float* d_coords,
+                                   gkCollisionPair* d_pairs, ogx_simplex_f32* d_simplices,
                                    float* d_distances, float* d_contact_normals);
 /* upload_pairs_device (GJK/gpu/openGJK.h:368) */
 ogx_status ogx_upload_pairs_device(int num_pairs, const gkCollisionPair* pairs,
                                    gkCollisionPair* d_pairs);
 /* compute_minimum_distance_indexed (GJK/gpu/openGJK.h:398) */
 ogx_status ogx_compute_minimum_distance_indexed(int num_polytopes, int num_pairs,
-                                                const gkPolytope* polytopes,
+                                                const ogx_polytope_f32* polytopes,
                                                 const gkCollisionPair* pairs,
-                                                gkSimplex* simplices, float* distances);
+                                                ogx_simplex_f32* simplices, float* distances);
 /* compute_minimum_distance_indexed_device (GJK/gpu/openGJK.h:419) */
-ogx_status ogx_compute_minimum_distance_indexed_device(int num_pairs, const gkPolytope* d_polytopes,
+ogx_status ogx_compute_minimum_distance_indexed_device(int num_pairs, const ogx_polytope_f32* d_polytopes,
                                                        const gkCollisionPair* d_pairs,
-                                                       gkSimplex* d_simplices, float* d_distances);
+                                                       ogx_simplex_f32* d_simplices, float* d_distances);
 /* compute_epa_indexed (GJK/gpu/openGJK.h:473): simplices/distances in/out */
-ogx_status ogx_compute_epa_indexed(int num_polytopes, int num_pairs, const gkPolytope* polytopes,
-                                   const gkCollisionPair* pairs, gkSimplex* simplices,
+ogx_status ogx_compute_epa_indexed(int num_polytopes, int num_pairs, const ogx_polytope_f32* polytopes,
+                                   const gkCollisionPair* pairs, ogx_simplex_f32* simplices,
                                    float* distances, float* contact_normals);
 /* compute_epa_indexed_device (GJK/gpu/openGJK.h:450) */
-ogx_status ogx_compute_epa_indexed_device(int num_pairs, const gkPolytope* d_polytopes,
-                                          const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
+ogx_status ogx_compute_epa_indexed_device(int num_pairs, const ogx_polytope_f32* d_polytopes,
+                                          const gkCollisionPair* d_pairs, ogx_simplex_f32* d_simplices,
                                           float* d_distances, float* d_contact_normals);
 /* compute_gjk_epa_indexed (GJK/gpu/openGJK.h:497) */
 ogx_status ogx_compute_gjk_epa_indexed(int num_polytopes, int num_pairs,
-                                       const gkPolytope* polytopes, const gkCollisionPair* pairs,
-                                       gkSimplex* simplices, float* distances,
+                                       const ogx_polytope_f32* polytopes, const gkCollisionPair* pairs,
+                                       ogx_simplex_f32* simplices, float* distances,
                                        float* contact_normals);
 /* GJK::GPU::timer() (examples/gpu/example.h:9): GPU milliseconds of the engine pipeline
- * of the last reference-compatible call on the current device. */
+ * of the calling thread's last reference-compatible call.  The calls above run on an
+ * engine context leased for the call (one per concurrent caller, kept for reuse), so calls
+ * from several host threads run side by side. */
 float ogx_compat_last_gpu_ms(void);
+
+/* The same calls for a caller built with the reference's USE_32BITS off
+ * (GJK/common.h:44-60: gkFloat = double, 48-byte gkPolytope, 184-byte gkSimplex).  The
+ * coordinates are rounded once to float and the FP32 engine runs on them; the results are
+ * widened to double, so they carry that input rounding (a relative 6e-8 per coordinate),
+ * not the rounding of an FP64 computation.  Host-buffer calls only: the device-buffer
+ * (*_device) functions take the FP32 layouts. */
+/* compute_minimum_distance (GJK/gpu/openGJK.h:91), FP64 layout */
+ogx_status ogx_compute_minimum_distance_f64(int n, const ogx_polytope_f64* bd1, const ogx_polytope_f64* bd2,
+                                            ogx_simplex_f64* simplices, double* distances);
+/* computeCollisionInformation(n, ...) (GJK/gpu/openGJK.h:112), FP64 layout */
+ogx_status ogx_compute_collision_information_f64(int n, const ogx_polytope_f64* bd1,
+                                                 const ogx_polytope_f64* bd2, ogx_simplex_f64* simplices,
+                                                 double* distances, double* contact_normals);
+/* compute_gjk_epa (GJK/gpu/openGJK.h:134), FP64 layout */
+ogx_status ogx_compute_gjk_epa_f64(int n, const ogx_polytope_f64* bd1, const ogx_polytope_f64* bd2,
+                                   ogx_simplex_f64* simplices, double* distances, double* contact_normals);
+/* GJK::GPU::computeCollisionInformation (README.md:39-46), FP64 layout */
+ogx_status ogx_compute_collision_information_witnesses_f64(int n, const ogx_polytope_f64* bd1,
+                                                           const ogx_polytope_f64* bd2,
+                                                           ogx_simplex_f64* simplices, double* distances,
+                                                           double* witness1, double* witness2,
+                                                           double* contact_normals);
+/* compute_minimum_distance_indexed (GJK/gpu/openGJK.h:398), FP64 layout */
+ogx_status ogx_compute_minimum_distance_indexed_f64(int num_polytopes, int num_pairs,
+                                                    const ogx_polytope_f64* polytopes,
+                                                    const gkCollisionPair* pairs, ogx_simplex_f64* simplices,
+                                                    double* distances);
+/* compute_epa_indexed (GJK/gpu/openGJK.h:473), FP64 layout */
+ogx_status ogx_compute_epa_indexed_f64(int num_polytopes, int num_pairs, const ogx_polytope_f64* polytopes,
+                                       const gkCollisionPair* pairs, ogx_simplex_f64* simplices,
+                                       double* distances, double* contact_normals);
+/* compute_gjk_epa_indexed (GJK/gpu/openGJK.h:497), FP64 layout */
+ogx_status ogx_compute_gjk_epa_indexed_f64(int num_polytopes, int num_pairs, const ogx_polytope_f64* polytopes,
+                                           const gkCollisionPair* pairs, ogx_simplex_f64* simplices,
+                                           double* distances, double* contact_normals);
 
 #ifdef __cplusplus
 }

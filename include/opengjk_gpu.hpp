@@ -10,8 +10,19 @@
 //   indexed API.
 // Like the reference, these functions return void; a failure throws ogx::Error (the
 // reference has no error reporting at all; silent failure is not reproduced).
+//
+// Precision: as the reference's USE_32BITS switch (GJK/common.h:44), gkFloat is float
+// unless OGX_GKFLOAT_DOUBLE is defined before this header (include/compat/GJK/common.h
+// defines it when USE_32BITS is not); then gkFloat is double, the types have the FP64
+// layouts, and the host-buffer and indexed calls go to the *_f64 entry points.  The
+// device-buffer (*_device) calls exist in the FP32 build only.
+//
+// A caller written against the reference keeps its includes: with include/compat and
+// include on the include path, "GJK/common.h", "GJK/gpu/openGJK.h" and
+// "examples/gpu/example.h" resolve to this header.
 #pragma once
 
+#include <chrono>
 #include <stdexcept>
 #include <string>
 
@@ -27,19 +38,27 @@ inline void check(ogx_status s) {
 }
 }  // namespace ogx
 
+// the C entry point of each call in the build's precision
+#ifdef OGX_GKFLOAT_DOUBLE
+#define OGX_PREC(name) name##_f64
+#else
+#define OGX_PREC(name) name
+#endif
+
 // ----- GJK/gpu/openGJK.h ---------------------------------------------------------------
 inline void compute_minimum_distance(const int n, const gkPolytope* bd1, const gkPolytope* bd2,
                                      gkSimplex* simplices, gkFloat* distances) {
-  ogx::check(ogx_compute_minimum_distance(n, bd1, bd2, simplices, distances));
+  ogx::check(OGX_PREC(ogx_compute_minimum_distance)(n, bd1, bd2, simplices, distances));
 }
 inline void computeCollisionInformation(const int n, const gkPolytope* bd1, const gkPolytope* bd2,
                                         gkSimplex* simplices, gkFloat* distances, gkFloat* contact_normals) {
-  ogx::check(ogx_compute_collision_information(n, bd1, bd2, simplices, distances, contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_collision_information)(n, bd1, bd2, simplices, distances, contact_normals));
 }
 inline void compute_gjk_epa(const int n, const gkPolytope* bd1, const gkPolytope* bd2, gkSimplex* simplices,
                             gkFloat* distances, gkFloat* contact_normals) {
-  ogx::check(ogx_compute_gjk_epa(n, bd1, bd2, simplices, distances, contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_gjk_epa)(n, bd1, bd2, simplices, distances, contact_normals));
 }
+#ifndef OGX_GKFLOAT_DOUBLE
 inline void allocate_epa_device_arrays(const int n, gkFloat** d_witness1, gkFloat** d_witness2,
                                        gkFloat** d_contact_normals) {
   ogx::check(ogx_allocate_epa_device_arrays(n, d_witness1, d_witness2, d_contact_normals));
@@ -88,21 +107,10 @@ inline void free_indexed_device(gkPolytope* d_polytopes, gkFloat* d_coords, gkCo
 inline void upload_pairs_device(const int num_pairs, const gkCollisionPair* pairs, gkCollisionPair* d_pairs) {
   ogx::check(ogx_upload_pairs_device(num_pairs, pairs, d_pairs));
 }
-inline void compute_minimum_distance_indexed(const int num_polytopes, const int num_pairs,
-                                             const gkPolytope* polytopes, const gkCollisionPair* pairs,
-                                             gkSimplex* simplices, gkFloat* distances) {
-  ogx::check(ogx_compute_minimum_distance_indexed(num_polytopes, num_pairs, polytopes, pairs, simplices, distances));
-}
 inline void compute_minimum_distance_indexed_device(const int num_pairs, const gkPolytope* d_polytopes,
                                                     const gkCollisionPair* d_pairs, gkSimplex* d_simplices,
                                                     gkFloat* d_distances) {
   ogx::check(ogx_compute_minimum_distance_indexed_device(num_pairs, d_polytopes, d_pairs, d_simplices, d_distances));
-}
-inline void compute_epa_indexed(const int num_polytopes, const int num_pairs, const gkPolytope* polytopes,
-                                const gkCollisionPair* pairs, gkSimplex* simplices, gkFloat* distances,
-                                gkFloat* contact_normals) {
-  ogx::check(ogx_compute_epa_indexed(num_polytopes, num_pairs, polytopes, pairs, simplices, distances,
-                                     contact_normals));
 }
 inline void compute_epa_indexed_device(const int num_pairs, const gkPolytope* d_polytopes,
                                        const gkCollisionPair* d_pairs, gkSimplex* d_simplices, gkFloat* d_distances,
@@ -110,19 +118,53 @@ inline void compute_epa_indexed_device(const int num_pairs, const gkPolytope* d_
   ogx::check(ogx_compute_epa_indexed_device(num_pairs, d_polytopes, d_pairs, d_simplices, d_distances,
                                             d_contact_normals));
 }
+#endif  // !OGX_GKFLOAT_DOUBLE: device-buffer calls
+inline void compute_minimum_distance_indexed(const int num_polytopes, const int num_pairs,
+                                             const gkPolytope* polytopes, const gkCollisionPair* pairs,
+                                             gkSimplex* simplices, gkFloat* distances) {
+  ogx::check(OGX_PREC(ogx_compute_minimum_distance_indexed)(num_polytopes, num_pairs, polytopes, pairs, simplices,
+                                                            distances));
+}
+inline void compute_epa_indexed(const int num_polytopes, const int num_pairs, const gkPolytope* polytopes,
+                                const gkCollisionPair* pairs, gkSimplex* simplices, gkFloat* distances,
+                                gkFloat* contact_normals) {
+  ogx::check(OGX_PREC(ogx_compute_epa_indexed)(num_polytopes, num_pairs, polytopes, pairs, simplices, distances,
+                                               contact_normals));
+}
 inline void compute_gjk_epa_indexed(const int num_polytopes, const int num_pairs, const gkPolytope* polytopes,
                                     const gkCollisionPair* pairs, gkSimplex* simplices, gkFloat* distances,
                                     gkFloat* contact_normals) {
-  ogx::check(ogx_compute_gjk_epa_indexed(num_polytopes, num_pairs, polytopes, pairs, simplices, distances,
-                                         contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_gjk_epa_indexed)(num_polytopes, num_pairs, polytopes, pairs, simplices, distances,
+                                                   contact_normals));
 }
 
 // ----- examples/gpu/example.h: GJK::GPU ------------------------------------------------
 namespace GJK {
 namespace GPU {
-// examples/common/timer.h PerformanceTimer subset: the GPU time of the last call.
-struct PerformanceTimer {
-  float getGpuElapsedTimeForPreviousOperation() const { return ogx_compat_last_gpu_ms(); }
+// The PerformanceTimer of examples/common/timer.h, as GJK::GPU::timer() returns it:
+// after a GJK::GPU call, getGpuElapsedTimeForPreviousOperation() is the GPU time of
+// that call's engine pipeline (CUDA events, as the reference times its kernels); a
+// caller's own startGpuTimer() / endGpuTimer() pair around other calls (the reference's
+// driver times its indexed calls so, examples/main.cpp:417-422) measures the host time
+// between them, which covers the GPU work because every call returns complete; the CPU
+// timer pair is the host clock.  One timer per process, like the reference's function-
+// static singleton.
+class PerformanceTimer {
+ public:
+  void startCpuTimer() { t_cpu_ = std::chrono::steady_clock::now(); }
+  void endCpuTimer() { cpu_ms_ = ms_since(t_cpu_); }
+  void startGpuTimer() { t_gpu_ = std::chrono::steady_clock::now(); }
+  void endGpuTimer() { gpu_ms_ = ms_since(t_gpu_); }
+  float getCpuElapsedTimeForPreviousOperation() const { return cpu_ms_; }
+  float getGpuElapsedTimeForPreviousOperation() const { return gpu_ms_; }
+  void record_last_call() { gpu_ms_ = ogx_compat_last_gpu_ms(); }
+
+ private:
+  static float ms_since(std::chrono::steady_clock::time_point t) {
+    return std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t).count();
+  }
+  std::chrono::steady_clock::time_point t_cpu_{}, t_gpu_{};
+  float cpu_ms_ = 0.0f, gpu_ms_ = 0.0f;
 };
 inline PerformanceTimer& timer() {
   static PerformanceTimer t;
@@ -130,21 +172,25 @@ inline PerformanceTimer& timer() {
 }
 inline void computeDistances(const int n, const gkPolytope* bd1, const gkPolytope* bd2, gkSimplex* simplices,
                              gkFloat* distances) {
-  ogx::check(ogx_compute_minimum_distance(n, bd1, bd2, simplices, distances));
+  ogx::check(OGX_PREC(ogx_compute_minimum_distance)(n, bd1, bd2, simplices, distances));
+  timer().record_last_call();
 }
 inline void computeEPA(const int n, const gkPolytope* bd1, const gkPolytope* bd2, gkSimplex* simplices,
                        gkFloat* distances, gkFloat* contact_normals) {
-  ogx::check(ogx_compute_collision_information(n, bd1, bd2, simplices, distances, contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_collision_information)(n, bd1, bd2, simplices, distances, contact_normals));
+  timer().record_last_call();
 }
 inline void computeGJKAndEPA(const int n, const gkPolytope* bd1, const gkPolytope* bd2, gkSimplex* simplices,
                              gkFloat* distances, gkFloat* contact_normals) {
-  ogx::check(ogx_compute_gjk_epa(n, bd1, bd2, simplices, distances, contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_gjk_epa)(n, bd1, bd2, simplices, distances, contact_normals));
+  timer().record_last_call();
 }
 inline void computeCollisionInformation(const int n, const gkPolytope* bd1, const gkPolytope* bd2,
                                         gkSimplex* simplices, gkFloat* distances, gkFloat* witness1,
                                         gkFloat* witness2, gkFloat* contact_normals = nullptr) {
-  ogx::check(ogx_compute_collision_information_witnesses(n, bd1, bd2, simplices, distances, witness1, witness2,
-                                                         contact_normals));
+  ogx::check(OGX_PREC(ogx_compute_collision_information_witnesses)(n, bd1, bd2, simplices, distances, witness1,
+                                                                   witness2, contact_normals));
+  timer().record_last_call();
 }
 }  // namespace GPU
 }  // namespace GJK

@@ -15,6 +15,7 @@
 namespace ogx {
 
 struct MemBodies {
+  static constexpr bool kExact64 = false;  // dpoint() is the float point widened
   const float* base[2];  // x[0] of each body
   int n[2];
   int n4[2];
@@ -119,9 +120,25 @@ struct MemBodies {
   }
 };
 
+// Bodies given in double by the caller (the FP64 drop-in): the pool holds their points
+// rounded to float, which the FP32 scans read; dpoint() reads the caller's double
+// coordinates (xyz interleaved, point i of body w at aos[w] + 3 i), so the FP64 steps run
+// on the exact inputs.
+struct D64Bodies : MemBodies {
+  static constexpr bool kExact64 = true;
+  const double* aos[2];
+  OGX_HD void bind64(const float* pool, BodyRef a, BodyRef b, const double* a64, const double* b64) {
+    bind(pool, a, b);
+    aos[0] = a64;
+    aos[1] = b64;
+  }
+  OGX_HD dv3 dpoint(int w, int i) const { return v3<double>(aos[w][3 * i], aos[w][3 * i + 1], aos[w][3 * i + 2]); }
+};
+
 #if defined(__CUDACC__)
 template <int L, int K>
 struct RegBodies {
+  static constexpr bool kExact64 = false;
   float4 x[2][K], y[2][K], z[2][K];
   MemBodies mem;  // for point() lookups by index
 

@@ -56,6 +56,14 @@ __global__ void k_box(const float* __restrict__ pool, const BodyRef* __restrict_
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int b = warp; b < n; b += nwarps) {
     const BodyRef r = bodies[b];
+    if (r.n < 1) {  // no points, or a NaN / infinite coordinate: the body takes no cell
+      if (lane == 0) {
+        lo[b] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+        hi[b] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        ncells[b] = 0;
+      }
+      continue;
+    }
     const int n4 = round4(r.n);
     const float* X = pool + 4 * (size_t)r.quad;
     float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};

@@ -15,6 +15,7 @@
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "ogx.h"
 
@@ -445,5 +446,17 @@ struct BodyRef {
 };
 
 OGX_HD int round4(int n) { return (n + 3) & ~3; }
+
+// A body whose points hold a NaN or an infinity is marked in the device body table by a
+// negated point count (set by the packing kernels); its layout is still that of |n|
+// points.  Kernels that lay out or copy a body use body_points(); the binning sees n < 1
+// and reports the body's pairs as bad input, so no query kernel ever reads it.
+OGX_HD int body_points(BodyRef r) { return r.n < 0 ? -r.n : r.n; }
+
+OGX_HD bool is_finite(float x) {
+  uint32_t u;
+  memcpy(&u, &x, sizeof u);
+  return (u & 0x7f800000u) != 0x7f800000u;
+}
 
 }  // namespace ogx

@@ -7,7 +7,9 @@
 // own kernels between calls).  Every call here copies the referenced bodies into the
 // engine's padded SoA pool (on the device: a count -> prefix-sum -> pack sequence), runs
 // the engine pipeline and, like the reference, returns when the results are complete.
-// The calls share one engine context per device (created on first use).
+// Each call leases an engine context of its own (stream, pool and result buffers) from a
+// per-device free list, created on first need: calls from several host threads run side
+// by side, and a thread's calls reuse warm contexts.
 //
 // Deliberate differences from the reference (documented bugs not reproduced):
 //  * computeCollisionInformation uploads the input distances (the reference does not,
@@ -131,7 +133,8 @@ __global__ void __launch_bounds__(kScanBlock) k_desc_offsets(DescSrc src, int nb
   }
 }
 
-__global__ void k_desc_pack(DescSrc src, int nb, const BodyRef* __restrict__ bodies, float* __restrict__ pool) {
+// bodies with a NaN or infinite coordinate are marked as k_pack does (negated count)
+__global__ void k_desc_pack(DescSrc src, int nb, BodyRef* __restrict__ bodies, float* __restrict__ pool) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -141,12 +144,50 @@ __global__ void k_desc_pack(DescSrc src, int nb, const BodyRef* __restrict__ bod
     const float* c = src.get(b).coord;
     const int n4 = round4(r.n);
     float* dst = pool + 4 * (size_t)r.quad;
+    bool finite = true;
     for (int i = lane; i < n4; i += 32) {
       const int s = i < r.n ? i : 0;
-      dst[i] = c[3 * s];
-      dst[n4 + i] = c[3 * s + 1];
-      dst[2 * n4 + i] = c[3 * s + 2];
+      const float x = c[3 * s], y = c[3 * s + 1], z = c[3 * s + 2];
+      finite = finite && is_finite(x) && is_finite(y) && is_finite(z);
+      dst[i] = x;
+      dst[n4 + i] = y;
+      dst[2 * n4 + i] = z;
     }
+    finite = __all_sync(0xffffffffu, finite);
+    if (lane == 0 && !finite) bodies[b].n = -r.n;
+  }
+}
+
+// Bodies given in double (the *_f64 calls): every separated pair continues GJK in FP64 on
+// the caller's double points from the FP32 pass's final simplex -- exact supports and
+// exact Minkowski points, one thread per pair -- so its distance carries no rounding of
+// the inputs; its simplex, witnesses and normal are replaced with the continuation's.
+// Contacts keep the FP32 pass's result (their depth is within the inputs' rounding of
+// the FP64 one, far inside the 1e-4 depth tolerance); a pair the continuation finds
+// enclosed lies within rounding of touching and keeps it too.
+__global__ void __launch_bounds__(128) k_refine64(const float* __restrict__ pool, const BodyRef* __restrict__ bodies,
+                                                  const double* __restrict__ c64, const int64_t* __restrict__ voff,
+                                                  const int2* __restrict__ pairs, int npairs, gkSimplex* smp,
+                                                  float* dist, float* nrm) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x) {
+    const float dp = dist[p];
+    if (!(dp > FLT_EPSILON)) continue;  // contacts, and bad input (NaN)
+    const int2 pr = pairs[p];
+    const BodyRef ra = bodies[pr.x], rb = bodies[pr.y];
+    if (ra.n < 1 || rb.n < 1) continue;
+    D64Bodies B;
+    B.bind64(pool, ra, rb, c64 + 3 * voff[pr.x], c64 + 3 * voff[pr.y]);
+    GjkState g;
+    load_simplex(smp + p, dp, g);
+    if (smp[p].nvrtx < 1 || smp[p].nvrtx > 3) continue;
+    g.certain = false;
+    g.status = 0;
+    SerialTeam t;
+    gjk_refine(t, B, g, kRefineIters);
+    if (gjk_contact(g)) continue;
+    store_simplex(smp + p, g);
+    dist[p] = g.dist;
+    if (nrm) store3(nrm + 3 * (size_t)p, sep_normal(g));
   }
 }
 
@@ -180,12 +221,16 @@ struct Compat {
   size_t dist_cap = 0;
   float* d_nrm = nullptr;
   size_t nrm_cap = 0;
+  double* d_c64 = nullptr;  // the *_f64 calls: the bodies' double coordinates, pool order
+  size_t c64_cap = 0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   float last_ms = 0.0f;
 };
 
-std::mutex g_compat_mu;
-Compat g_compat[16];
+constexpr int kMaxDevices = 16;
+std::mutex g_compat_mu;  // guards the free lists
+std::vector<Compat*> g_free[kMaxDevices];
+thread_local float t_last_ms = 0.0f;  // GPU time of this thread's last call
 
 template <class T>
 ogx_status grow(T** p, size_t* cap, size_t need, const char* what) {
@@ -200,22 +245,46 @@ ogx_status grow(T** p, size_t* cap, size_t need, const char* what) {
   return OGX_OK;
 }
 
-ogx_status compat(Compat** out) {
+// A context leased for the duration of one call; back on its device's free list after.
+struct Lease {
+  Compat* c = nullptr;
+  int dev = 0;
+  Lease() = default;
+  Lease(const Lease&) = delete;
+  Lease& operator=(const Lease&) = delete;
+  ~Lease() {
+    if (!c) return;
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    g_free[dev].push_back(c);
+  }
+};
+
+ogx_status lease(Lease& L) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return ogx_fail(OGX_ERR_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
   }
-  if (dev >= 16) return ogx_fail(OGX_ERR_INVALID, "device index %d", dev);
-  Compat& c = g_compat[dev];
-  if (!c.ctx) {
-    ogx_status s = ogx_ctx_create(dev, nullptr, nullptr, &c.ctx);
-    if (s) return s;
-    cudaEventCreate(&c.t0);
-    cudaEventCreate(&c.t1);
+  if (dev < 0 || dev >= kMaxDevices) return ogx_fail(OGX_ERR_INVALID, "device index %d", dev);
+  L.dev = dev;
+  {
+    std::lock_guard<std::mutex> lk(g_compat_mu);
+    if (!g_free[dev].empty()) {
+      L.c = g_free[dev].back();
+      g_free[dev].pop_back();
+      return OGX_OK;
+    }
   }
-  *out = &c;
+  Compat* c = new Compat();
+  ogx_status s = ogx_ctx_create(dev, nullptr, nullptr, &c->ctx);
+  if (s) {
+    delete c;
+    return s;
+  }
+  cudaEventCreate(&c->t0);
+  cudaEventCreate(&c->t1);
+  L.c = c;
   return OGX_OK;
 }
 
@@ -313,15 +382,24 @@ ogx_status ensure_results(Compat& c, int n) {
 }
 
 ogx_status run_timed(Compat& c, int nbodies, int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp,
-                     float* d_dist, float* d_nrm, int mode) {
+                     float* d_dist, float* d_nrm, int mode, bool exact64 = false) {
   cudaEventRecord(c.t0, c.ctx->stream);
   ogx_status s = ogx_run(c.ctx, c.d_points, c.d_bodies, nbodies, npairs, d_pairs, d_smp, d_dist, d_nrm,
                          nullptr, mode);
+  if (!s && exact64 && mode != kModeEpa) {
+    const int grid = std::min(8 * c.ctx->sm_count, (npairs + 127) / 128);
+    k_refine64<<<std::max(grid, 1), 128, 0, c.ctx->stream>>>(c.d_points, c.d_bodies, c.d_c64, c.d_voff,
+                                                            reinterpret_cast<const int2*>(d_pairs), npairs,
+                                                            d_smp, d_dist, mode == kModeGjk ? nullptr : d_nrm);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = ogx_cuda_fail(e, "k_refine64 launch");
+  }
   cudaEventRecord(c.t1, c.ctx->stream);
   if (s) return s;
   cudaError_t e = cudaStreamSynchronize(c.ctx->stream);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "engine pipeline");
   cudaEventElapsedTime(&c.last_ms, c.t0, c.t1);
+  t_last_ms = c.last_ms;
   return OGX_OK;
 }
 
@@ -334,18 +412,31 @@ ogx_status finish(Compat& c) {
 // host-buffer query over pairs (2i, 2i+1) or explicit pairs; results to host arrays
 ogx_status host_query(const gkPolytope* a, const gkPolytope* b, int nbodies, int npairs,
                       const gkCollisionPair* host_pairs, gkSimplex* smp, float* dist, float* nrm,
-                      float* w1, float* w2, int mode, bool upload_in) {
+                      float* w1, float* w2, int mode, bool upload_in, const ogx_polytope_f64* a64 = nullptr,
+                      const ogx_polytope_f64* b64 = nullptr) {
   if (npairs <= 0) return OGX_OK;  // the reference returns early for n <= 0
   if (!a || !smp || !dist) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
-  std::lock_guard<std::mutex> lk(g_compat_mu);
-  Compat* c;
-  ogx_status s = compat(&c);
+  Lease L;
+  ogx_status s = lease(L);
   if (s) return s;
+  Compat* c = L.c;
   cudaStream_t st = c->ctx->stream;
   s = pool_from_host_desc(*c, a, b, nbodies);
   if (!s) s = ensure_results(*c, npairs);
   if (s) return s;
-  cudaError_t e;
+  std::vector<double> c64;
+  if (a64) {
+    // the double coordinates in the pool's body order (body i as pool_from_host_desc)
+    for (int i = 0; i < nbodies; ++i) {
+      const ogx_polytope_f64& p = b64 ? ((i & 1) ? b64[i >> 1] : a64[i >> 1]) : a64[i];
+      c64.insert(c64.end(), p.coord, p.coord + 3 * (size_t)p.numpoints);
+    }
+    s = grow(&c->d_c64, &c->c64_cap, std::max<size_t>(c64.size(), 1), "compat double coordinates");
+    if (s) return s;
+  }
+  cudaError_t e = cudaSuccess;
+  if (a64) e = cudaMemcpyAsync(c->d_c64, c64.data(), c64.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "double coordinate upload");
   if (host_pairs) {
     for (int i = 0; i < npairs; ++i)
       if (host_pairs[i].idx1 < 0 || host_pairs[i].idx1 >= nbodies || host_pairs[i].idx2 < 0 ||
@@ -361,7 +452,7 @@ ogx_status host_query(const gkPolytope* a, const gkPolytope* b, int nbodies, int
     if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_dist, dist, npairs * sizeof(float), cudaMemcpyHostToDevice, st);
   }
   if (e != cudaSuccess) return ogx_cuda_fail(e, "input upload");
-  s = run_timed(*c, nbodies, npairs, c->d_pairs, c->d_smp, c->d_dist, c->d_nrm, mode);
+  s = run_timed(*c, nbodies, npairs, c->d_pairs, c->d_smp, c->d_dist, c->d_nrm, mode, a64 != nullptr);
   if (s) return s;
   e = cudaMemcpyAsync(smp, c->d_smp, npairs * sizeof(gkSimplex), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dist, c->d_dist, npairs * sizeof(float), cudaMemcpyDeviceToHost, st);
@@ -385,10 +476,10 @@ ogx_status device_query(DescSrc src, int nbodies, int npairs, gkSimplex* d_smp, 
                         int mode) {
   if (npairs <= 0) return OGX_OK;
   if (!src.a || !d_smp || !d_dist) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
-  std::lock_guard<std::mutex> lk(g_compat_mu);
-  Compat* c;
-  ogx_status s = compat(&c);
+  Lease L;
+  ogx_status s = lease(L);
   if (s) return s;
+  Compat* c = L.c;
   s = pool_from_device_desc(*c, src, nbodies);
   if (s) return s;
   s = ensure_results(*c, npairs);
@@ -664,9 +755,173 @@ extern "C" ogx_status ogx_compute_gjk_epa_indexed(int num_polytopes, int num_pai
 }
 
 // GJK::GPU::timer() (examples/gpu/example.h:9): GPU time of the engine pipeline of the
-// last reference-compatible call on the current device, in milliseconds.
-extern "C" float ogx_compat_last_gpu_ms(void) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev >= 16) return 0.0f;
-  return g_compat[dev].last_ms;
+// calling thread's last reference-compatible call, in milliseconds.
+extern "C" float ogx_compat_last_gpu_ms(void) { return t_last_ms; }
+
+// =================================================================================
+// FP64 layouts (the reference built with USE_32BITS off, GJK/common.h:44-60).  The
+// coordinates are rounded once to float, the engine runs on them as on any FP32 input,
+// and the results are widened to double: they carry the rounding of the inputs (a
+// relative 6e-8 of each coordinate), not that of an FP64 computation.
+
+namespace {
+
+// FP32 copies of FP64 descriptor arrays: one float coordinate buffer, descriptors into it
+struct Narrowed {
+  std::vector<float> coords;
+  std::vector<gkPolytope> a, b;
+};
+
+ogx_status narrow_desc(const ogx_polytope_f64* src, int n, std::vector<gkPolytope>& out, std::vector<float>& coords,
+                       std::vector<int64_t>& first) {
+  out.resize(n);
+  for (int i = 0; i < n; ++i) {
+    if (src[i].numpoints < 1 || !src[i].coord)
+      return ogx_fail(OGX_ERR_INVALID, "polytope %d: numpoints %d, coord %p", i, src[i].numpoints,
+                      (void*)src[i].coord);
+    first.push_back((int64_t)coords.size());
+    for (int k = 0; k < 3 * src[i].numpoints; ++k) coords.push_back((float)src[i].coord[k]);
+    out[i].numpoints = src[i].numpoints;
+    for (int k = 0; k < 3; ++k) out[i].s[k] = (float)src[i].s[k];
+    out[i].s_idx = src[i].s_idx;
+    out[i].coord = nullptr;  // set once the buffer stops growing
+  }
+  return OGX_OK;
+}
+
+ogx_status narrow(int na, const ogx_polytope_f64* a, int nb, const ogx_polytope_f64* b, Narrowed& N) {
+  std::vector<int64_t> fa, fb;
+  ogx_status s = narrow_desc(a, na, N.a, N.coords, fa);
+  if (!s && b) s = narrow_desc(b, nb, N.b, N.coords, fb);
+  if (s) return s;
+  for (int i = 0; i < na; ++i) N.a[i].coord = N.coords.data() + fa[i];
+  for (int i = 0; b && i < nb; ++i) N.b[i].coord = N.coords.data() + fb[i];
+  return OGX_OK;
+}
+
+void narrow_simplex(const ogx_simplex_f64& d, gkSimplex& f) {
+  f.nvrtx = d.nvrtx;
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) f.vrtx[k][c] = (float)d.vrtx[k][c];
+  for (int k = 0; k < 4; ++k) {
+    f.vrtx_idx[k][0] = d.vrtx_idx[k][0];
+    f.vrtx_idx[k][1] = d.vrtx_idx[k][1];
+  }
+  for (int w = 0; w < 2; ++w)
+    for (int c = 0; c < 3; ++c) f.witnesses[w][c] = (float)d.witnesses[w][c];
+}
+
+void widen_simplex(const gkSimplex& f, ogx_simplex_f64& d) {
+  d.nvrtx = f.nvrtx;
+  for (int k = 0; k < 4; ++k)
+    for (int c = 0; c < 3; ++c) d.vrtx[k][c] = f.vrtx[k][c];
+  for (int k = 0; k < 4; ++k) {
+    d.vrtx_idx[k][0] = f.vrtx_idx[k][0];
+    d.vrtx_idx[k][1] = f.vrtx_idx[k][1];
+  }
+  for (int w = 0; w < 2; ++w)
+    for (int c = 0; c < 3; ++c) d.witnesses[w][c] = f.witnesses[w][c];
+}
+
+// host_query on FP64 arrays: pairs (a[i], b[i]) when b is given, else pairs into a
+ogx_status host_query_f64(const ogx_polytope_f64* a, const ogx_polytope_f64* b, int nbodies, int npairs,
+                          const gkCollisionPair* pairs, ogx_simplex_f64* smp, double* dist, double* nrm,
+                          double* w1, double* w2, int mode, bool upload_in) {
+  if (npairs <= 0) return OGX_OK;
+  if (!a || !smp || !dist) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  Narrowed N;
+  ogx_status s = b ? narrow(npairs, a, npairs, b, N) : narrow(nbodies, a, 0, nullptr, N);
+  if (s) return s;
+  std::vector<gkSimplex> s32(npairs);
+  std::vector<float> d32(npairs), n32(nrm ? 3 * (size_t)npairs : 0);
+  std::vector<float> w32a(w1 ? 3 * (size_t)npairs : 0), w32b(w2 ? 3 * (size_t)npairs : 0);
+  if (upload_in)
+    for (int i = 0; i < npairs; ++i) {
+      narrow_simplex(smp[i], s32[i]);
+      d32[i] = (float)dist[i];
+    }
+  s = host_query(N.a.data(), b ? N.b.data() : nullptr, nbodies, npairs, pairs, s32.data(), d32.data(),
+                 nrm ? n32.data() : nullptr, w1 ? w32a.data() : nullptr, w2 ? w32b.data() : nullptr, mode,
+                 upload_in, a, b);
+  if (s) return s;
+  for (int i = 0; i < npairs; ++i) {
+    widen_simplex(s32[i], smp[i]);
+    dist[i] = d32[i];
+  }
+  for (size_t k = 0; k < n32.size(); ++k) nrm[k] = n32[k];
+  for (size_t k = 0; k < w32a.size(); ++k) w1[k] = w32a[k];
+  for (size_t k = 0; k < w32b.size(); ++k) w2[k] = w32b[k];
+  return OGX_OK;
+}
+
+}  // namespace
+
+// compute_minimum_distance / GJK::GPU::computeDistances with gkFloat = double
+extern "C" ogx_status ogx_compute_minimum_distance_f64(int n, const ogx_polytope_f64* bd1,
+                                                       const ogx_polytope_f64* bd2, ogx_simplex_f64* simplices,
+                                                       double* distances) {
+  if (n > 0 && !bd2) return ogx_fail(OGX_ERR_INVALID, "bd2 is NULL");
+  return host_query_f64(bd1, bd2, 2 * n, n, nullptr, simplices, distances, nullptr, nullptr, nullptr, kModeGjk,
+                        false);
+}
+
+// computeCollisionInformation(n, ...) / GJK::GPU::computeEPA with gkFloat = double
+extern "C" ogx_status ogx_compute_collision_information_f64(int n, const ogx_polytope_f64* bd1,
+                                                            const ogx_polytope_f64* bd2,
+                                                            ogx_simplex_f64* simplices, double* distances,
+                                                            double* contact_normals) {
+  if (n > 0 && !bd2) return ogx_fail(OGX_ERR_INVALID, "bd2 is NULL");
+  return host_query_f64(bd1, bd2, 2 * n, n, nullptr, simplices, distances, contact_normals, nullptr, nullptr,
+                        kModeEpa, true);
+}
+
+// compute_gjk_epa / GJK::GPU::computeGJKAndEPA with gkFloat = double
+extern "C" ogx_status ogx_compute_gjk_epa_f64(int n, const ogx_polytope_f64* bd1, const ogx_polytope_f64* bd2,
+                                              ogx_simplex_f64* simplices, double* distances,
+                                              double* contact_normals) {
+  if (n > 0 && !bd2) return ogx_fail(OGX_ERR_INVALID, "bd2 is NULL");
+  return host_query_f64(bd1, bd2, 2 * n, n, nullptr, simplices, distances, contact_normals, nullptr, nullptr,
+                        kModeGjkEpa, false);
+}
+
+// GJK::GPU::computeCollisionInformation (README.md:39-46 form) with gkFloat = double
+extern "C" ogx_status ogx_compute_collision_information_witnesses_f64(
+    int n, const ogx_polytope_f64* bd1, const ogx_polytope_f64* bd2, ogx_simplex_f64* simplices,
+    double* distances, double* witness1, double* witness2, double* contact_normals) {
+  if (n > 0 && !bd2) return ogx_fail(OGX_ERR_INVALID, "bd2 is NULL");
+  return host_query_f64(bd1, bd2, 2 * n, n, nullptr, simplices, distances, contact_normals, witness1, witness2,
+                        kModeEpa, true);
+}
+
+// compute_minimum_distance_indexed with gkFloat = double
+extern "C" ogx_status ogx_compute_minimum_distance_indexed_f64(int num_polytopes, int num_pairs,
+                                                               const ogx_polytope_f64* polytopes,
+                                                               const gkCollisionPair* pairs,
+                                                               ogx_simplex_f64* simplices, double* distances) {
+  if (num_polytopes <= 0 || num_pairs <= 0) return OGX_OK;
+  if (!pairs) return ogx_fail(OGX_ERR_INVALID, "pairs is NULL");
+  return host_query_f64(polytopes, nullptr, num_polytopes, num_pairs, pairs, simplices, distances, nullptr,
+                        nullptr, nullptr, kModeGjk, false);
+}
+
+// compute_epa_indexed with gkFloat = double: simplices/distances in/out
+extern "C" ogx_status ogx_compute_epa_indexed_f64(int num_polytopes, int num_pairs,
+                                                  const ogx_polytope_f64* polytopes, const gkCollisionPair* pairs,
+                                                  ogx_simplex_f64* simplices, double* distances,
+                                                  double* contact_normals) {
+  if (num_polytopes <= 0 || num_pairs <= 0) return OGX_OK;
+  if (!pairs) return ogx_fail(OGX_ERR_INVALID, "pairs is NULL");
+  return host_query_f64(polytopes, nullptr, num_polytopes, num_pairs, pairs, simplices, distances,
+                        contact_normals, nullptr, nullptr, kModeEpa, true);
+}
+
+// compute_gjk_epa_indexed with gkFloat = double
+extern "C" ogx_status ogx_compute_gjk_epa_indexed_f64(int num_polytopes, int num_pairs,
+                                                      const ogx_polytope_f64* polytopes,
+                                                      const gkCollisionPair* pairs, ogx_simplex_f64* simplices,
+                                                      double* distances, double* contact_normals) {
+  if (num_polytopes <= 0 || num_pairs <= 0) return OGX_OK;
+  if (!pairs) return ogx_fail(OGX_ERR_INVALID, "pairs is NULL");
+  return host_query_f64(polytopes, nullptr, num_polytopes, num_pairs, pairs, simplices, distances,
+                        contact_normals, nullptr, nullptr, kModeGjkEpa, false);
 }

@@ -88,6 +88,13 @@ OGX_HD double4* plane64_slot(Mem&, int) { return nullptr; }
 // the closest face by at most kEpaCertTol * max(1, scale).
 constexpr float kEpaCertGain = 2.5e-7f;
 constexpr double kEpaCertTol = 1e-10;
+// Thin contacts: the closest face within kEpaThin * scale of the origin (thin bodies such
+// as 1e-4-thick disks, or barely overlapping ones).  Their long, flat faces carry FP32
+// normals whose rounding (~1e-6) can hide a support that improves on the face by more
+// than the FP32 convergence tolerance; at FP32 convergence such a contact is checked with
+// exact supports along its face's FP64 plane and run again certified if they improve on
+// the face by more than that tolerance.
+constexpr float kEpaThin = 1e-3f;
 constexpr double kEpaCertVis = 1e-12;
 
 struct EpaOut {
@@ -110,6 +117,39 @@ OGX_HD fv3 unit_or_x(fv3 d) {
   return v3<float>(1.0f, 0.0f, 0.0f);
 }
 
+// Normal of a separated pair: the reference's normalize(w1 - w0) with (1,0,0) when the
+// witnesses coincide (GJK/cpu/EPA.c:350-360).  In exact arithmetic w1 - w0 = -v, v the
+// closest point of the Minkowski difference to the origin, and the normal is computed
+// from -v: v carries the accuracy of the distance (each component rounded relative to
+// itself), while the difference of two FP32 witnesses keeps their absolute rounding, a
+// few 1e-7 of the coordinates, which is more than 1e-4 of a distance below ~1e-3.
+OGX_HD fv3 sep_normal(const GjkState& g) { return unit_or_x(-g.v); }
+
+// The same normal from a GJK simplex given by a caller (EPA-only calls): v is re-solved
+// from the simplex's points of the two bodies (exact Minkowski differences, closest point
+// in double-float, as the certified re-solve of the GJK pass does); where the simplex's
+// vertex indices do not address the bodies, the reference's rule on the given witnesses.
+OGX_HD fv3 simplex_sep_normal(const MemBodies& B, const gkSimplex& s) {
+  const int n = s.nvrtx;
+  bool ok = n >= 1 && n <= 3;
+  xv3 P[3];
+  for (int j = 0; j < 3; ++j) {
+    if (!ok || j >= n) break;
+    const int ia = s.vrtx_idx[j][0], ib = s.vrtx_idx[j][1];
+    ok = ia >= 0 && ia < B.n[0] && ib >= 0 && ib < B.n[1];
+    if (ok) P[j] = xdiff(B.point(0, ia), B.point(1, ib));
+  }
+  if (ok) {
+    df lam[4];
+    xv3 v;
+    closest_on_simplex_t<df>(n, P, lam, v);
+    return unit_or_x(v3<float>(-to_float(v.x), -to_float(v.y), -to_float(v.z)));
+  }
+  const fv3 w0 = v3<float>(s.witnesses[0][0], s.witnesses[0][1], s.witnesses[0][2]);
+  const fv3 w1 = v3<float>(s.witnesses[1][0], s.witnesses[1][1], s.witnesses[1][2]);
+  return unit_or_x(w1 - w0);
+}
+
 // support of the Minkowski difference along d (first maximum wins, EPA.c:307-344)
 template <class Team, class Bodies>
 OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
@@ -119,6 +159,21 @@ OGX_HD fv3 msupport(const Team& t, const Bodies& B, fv3 d, int& ia, int& ib) {
   t.argmax(ba, ia);
   t.argmax(bb, ib);
   return B.point(0, ia) - B.point(1, ib);
+}
+
+// FP64 plane (unit normal, offset) of live face f from its exact points; w = INFINITY
+// for a degenerate face
+template <class Mem, class Bodies>
+OGX_HD double4 face_plane64(const Mem& M, const Bodies& B, int f) {
+  const int a = M.fv[f][0], b = M.fv[f][1], c = M.fv[f][2];
+  const dv3 q0 = B.dpoint(0, M.vid[a].x) - B.dpoint(1, M.vid[a].y);
+  const dv3 q1 = B.dpoint(0, M.vid[b].x) - B.dpoint(1, M.vid[b].y);
+  const dv3 q2 = B.dpoint(0, M.vid[c].x) - B.dpoint(1, M.vid[c].y);
+  const dv3 m = cross(q1 - q0, q2 - q0);
+  const double mm = dot(m, m);
+  if (!(mm > 0.0)) return make_double4_(0.0, 0.0, 0.0, (double)INFINITY);
+  const double inv = 1.0 / sqrt(mm);
+  return make_double4_(m.x * inv, m.y * inv, m.z * inv, dot(m, q0) * inv);
 }
 
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
@@ -217,7 +272,11 @@ OGX_HD int tri_weights(fv3 p0, fv3 p1, fv3 p2, float* l) {
 // contact is split into coplanar triangles), the neighbour that holds the projection is
 // used, so that w0 - w1 = depth * normal holds.
 template <class Mem, class Bodies>
-OGX_HD void epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o) {
+// With report_closer, returns true when a neighbour of the closest face is closer than it
+// in FP64 (the FP32 planes ranked the two wrongly): nothing is emitted then and the
+// caller runs the contact again with FP64 planes; without, the closest face's own result
+// is emitted in that case.
+OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o, bool report_closer) {
   int a = M.fv[f][0], b = M.fv[f][1], c = M.fv[f][2];
   float l[3];
   for (int hop = 0; hop < 4; ++hop) {
@@ -230,10 +289,24 @@ OGX_HD void epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o)
     if (out < 0) break;
     const int g2 = M.fa[f][out];
     const float4 nf = M.fn[f], ng = M.fn[g2];
-    const bool coplanar = M.fv[g2][3] && fabsf(ng.w - nf.w) <= tie &&
-                          (nf.x * ng.x + nf.y * ng.y + nf.z * ng.z) > 1.0f - 1e-5f;
-    if (!coplanar) break;
-    f = g2;
+    const bool near = M.fv[g2][3] && fabsf(ng.w - nf.w) <= tie &&
+                      (nf.x * ng.x + nf.y * ng.y + nf.z * ng.z) > 1.0f - 1e-5f;
+    if (!near) break;
+    // In exact arithmetic the origin projects into the closest face of the convex
+    // polytope, so the neighbour it leaves through is either coplanar with it (a flat
+    // patch split into triangles: the witnesses come from the neighbour) or closer (the
+    // FP32 planes ranked the two wrongly).  Decided on FP64 planes of the exact points:
+    // a neighbour that is neither -- a few 1e-5 off, on dense flat patches -- is not a
+    // supporting plane, and the projection leaves the closest face by rounding only.
+    const double4 pf = face_plane64(M, B, f), pg = face_plane64(M, B, g2);
+    const double dn = ::fabs(pf.x - pg.x) + ::fabs(pf.y - pg.y) + ::fabs(pf.z - pg.z);
+    const double sc = ::fmax(1.0, ::fabs(pf.w));
+    if (dn <= 1e-9 && ::fabs(pg.w - pf.w) <= 1e-12 * sc) {
+      f = g2;
+      continue;
+    }
+    if (report_closer && pg.w < pf.w - 1e-12 * sc) return true;
+    break;
   }
   const int2 ia = M.vid[a], ib = M.vid[b], ic = M.vid[c];
   o.w0 = B.point(0, ia.x) * l[0] + B.point(0, ib.x) * l[1] + B.point(0, ic.x) * l[2];
@@ -247,6 +320,7 @@ OGX_HD void epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o)
   o.face[1][1] = ib.y;
   o.face[2][0] = ic.x;
   o.face[2][1] = ic.y;
+  return false;
 }
 
 OGX_HD void epa_touch(fv3 a, fv3 b, EpaOut& o) {
@@ -574,6 +648,17 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       const float tol = fmaxf(tol_floor, cfg.epa_rel * scale);
       gain = dot(n, q) - bd;
       conv = gain < tol;
+      if (conv && !all64 && escalate && can_spill && !(gain > kEpaCertGain * scale) && bd < kEpaThin * scale) {
+        // a thin contact: the FP32 test may have been fooled by the face normal's rounding
+        const double4 p = face_plane64(M, B, best);
+        if (p.w < (double)INFINITY) {
+          const dv3 n64 = v3<double>(p.x, p.y, p.z);
+          double ha, hb;
+          exact_support(t, B, 0, n64, ha);
+          exact_support(t, B, 1, -n64, hb);
+          if (ha + hb - p.w > (double)tol) gain = INFINITY;  // re-run certified below
+        }
+      }
     }
     if (conv) {
       if (!cert && escalate && can_spill && !all64 && gain > kEpaCertGain * scale) {
@@ -766,7 +851,12 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     o.status |= OGX_S_EPA_CAP;
   }
   if (best >= 0) {
-    epa_emit(M, B, best, fmaxf(cfg.epa_tol, cfg.epa_rel * sqrtf(scale2)), o);
+    const bool rerun = !cert && escalate && can_spill && !all64;
+    if (epa_emit(M, B, best, fmaxf(cfg.epa_tol, cfg.epa_rel * sqrtf(scale2)), o, rerun)) {
+      o.spill = true;
+      o.spill64 = true;
+      return;
+    }
     o.polish = (cfg.flags & OGX_F_FP64_POLISH) != 0;
   }
 }

@@ -774,9 +774,11 @@ OGX_HD void gjk_end(const Team& t, const Bodies& B, const Config& cfg, const Gjk
   g.certain = false;
   g.wa = ia;
   g.wb = ib;
-  if ((cfg.flags & OGX_F_FP64_POLISH) && g.n >= 2 && g.n <= 3 && !gjk_contact(g)) {
+  if ((cfg.flags & OGX_F_FP64_POLISH) && g.n >= 1 && g.n <= 3 && !gjk_contact(g)) {
     const float errb = 16.0f * FLT_EPSILON * sqrtf(g.wmax2);
-    g.polish = errb > cfg.polish_rel * g.dist;
+    // a pair that ran into the iteration cap did not converge (the region decisions can
+    // cycle): its FP64 continuation decides it
+    g.polish = (g.n >= 2 && errb > cfg.polish_rel * g.dist) || g.exit == GJK_EXIT_CAP;
   }
   if (g.polish) {
     // Is the exact support along the exact closest point v64 one of the final simplex's
@@ -837,13 +839,22 @@ OGX_HD int exact_support(const Team& t, const Bodies& B, int w, vec3<T> d, T& va
   }
   m = t.fmax_(m);
   amax = t.fmax_(amax);
-  const float e = 4.0f * FLT_EPSILON * amax * (fabsf(fd.x) + fabsf(fd.y) + fabsf(fd.z)) + FLT_MIN;
+  // bodies given in double: the float points are the inputs rounded (half an ulp each),
+  // one more FLT_EPSILON * amax * |d|_1 of difference to cover
+  const float ef = Bodies::kExact64 ? 5.0f : 4.0f;
+  const float e = ef * FLT_EPSILON * amax * (fabsf(fd.x) + fabsf(fd.y) + fabsf(fd.z)) + FLT_MIN;
   const float lo = m - 2.0f * e;
   T best = sc<T>(-INFINITY);
   int bi = 0x7fffffff;
   for (int i = t.lane(); i < n; i += Team::L) {
     if (sdot(X[i], Y[i], Z[i], fd) < lo) continue;
-    const T x = sc<T>(X[i]) * d.x + sc<T>(Y[i]) * d.y + sc<T>(Z[i]) * d.z;
+    T x;
+    if constexpr (Bodies::kExact64) {
+      const dv3 p = B.dpoint(w, i);
+      x = p.x * d.x + p.y * d.y + p.z * d.z;
+    } else {
+      x = sc<T>(X[i]) * d.x + sc<T>(Y[i]) * d.y + sc<T>(Z[i]) * d.z;
+    }
     if (x > best || (x == best && i < bi)) {
       best = x;
       bi = i;
@@ -941,6 +952,103 @@ OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, Refin
   r.done = r.it >= max_iter;
 }
 
+// Closest point of a simplex to the origin by exhaustive search (Johnson's method without
+// the region tests): every sub-simplex that holds the newest vertex s.v[s.n-1] is solved
+// on its affine hull (Gram system), those whose barycentric weights are all >= 0 are
+// feasible, and the feasible one nearest the origin wins (fewer vertices on ties).  In
+// exact arithmetic the closest point after a GJK step lies on such a sub-simplex.  Cold
+// path: taken when the signed-volume region decisions made no progress -- on some
+// configurations the hff tests of the reference's sub-distance (GJK/cpu/openGJK.c:315-613)
+// pick a region whose point is farther than the last one, and GJK then cycles until its
+// iteration cap (the reference's own FP64 code does so on a pair of the 1M-pair power-law
+// batch and returns a distance 1.3% too large).  Returns the reduced simplex in s (slots
+// keep their .k) and its closest point in v; s.n == 4 means the origin is enclosed.
+template <class T>
+#if defined(__CUDACC__)
+__noinline__
+#endif
+OGX_HD void closest_exhaustive(Sx<T>& s, vec3<T>& v) {
+  const int n = s.n;
+  const int nw = n - 1;
+  const T zero = T(0);
+  T best = T(INFINITY);
+  int best_mask = 1 << nw, best_k = 5;
+  vec3<T> best_v = s.v[nw].p;
+  for (int mask = 1; mask < (1 << n); ++mask) {
+    if (!(mask & (1 << nw))) continue;
+    int idx[4], k = 0;
+    idx[k++] = nw;  // the newest vertex first
+    for (int j = 0; j < n; ++j)
+      if (j != nw && (mask & (1 << j))) idx[k++] = j;
+    const vec3<T> p0 = s.v[idx[0]].p;
+    T lam[4] = {T(1), zero, zero, zero};
+    bool ok = true;
+    if (k >= 2) {
+      vec3<T> e[3];
+      for (int a = 1; a < k; ++a) e[a - 1] = s.v[idx[a]].p - p0;
+      const int m = k - 1;
+      T G[3][3], r[3];
+      for (int a = 0; a < m; ++a) {
+        r[a] = -dot(p0, e[a]);
+        for (int c = 0; c < m; ++c) G[a][c] = dot(e[a], e[c]);
+      }
+      T x[3] = {zero, zero, zero};
+      if (m == 1) {
+        ok = G[0][0] > zero;
+        if (ok) x[0] = r[0] / G[0][0];
+      } else if (m == 2) {
+        const T det = G[0][0] * G[1][1] - G[0][1] * G[1][0];
+        ok = det > zero;
+        if (ok) {
+          x[0] = (r[0] * G[1][1] - G[0][1] * r[1]) / det;
+          x[1] = (G[0][0] * r[1] - r[0] * G[1][0]) / det;
+        }
+      } else {
+        // x = adj(G) r / det(G), adj(G)[i][j] = C[j][i] with C the cofactor matrix
+        T C[3][3];
+        C[0][0] = G[1][1] * G[2][2] - G[1][2] * G[2][1];
+        C[0][1] = G[1][2] * G[2][0] - G[1][0] * G[2][2];
+        C[0][2] = G[1][0] * G[2][1] - G[1][1] * G[2][0];
+        C[1][0] = G[0][2] * G[2][1] - G[0][1] * G[2][2];
+        C[1][1] = G[0][0] * G[2][2] - G[0][2] * G[2][0];
+        C[1][2] = G[0][1] * G[2][0] - G[0][0] * G[2][1];
+        C[2][0] = G[0][1] * G[1][2] - G[0][2] * G[1][1];
+        C[2][1] = G[0][2] * G[1][0] - G[0][0] * G[1][2];
+        C[2][2] = G[0][0] * G[1][1] - G[0][1] * G[1][0];
+        const T det = G[0][0] * C[0][0] + G[0][1] * C[0][1] + G[0][2] * C[0][2];
+        ok = det > zero;
+        if (ok)
+          for (int a = 0; a < 3; ++a) x[a] = (C[0][a] * r[0] + C[1][a] * r[1] + C[2][a] * r[2]) / det;
+      }
+      T sum = zero;
+      for (int a = 0; a < m; ++a) {
+        lam[a + 1] = x[a];
+        sum = sum + x[a];
+      }
+      lam[0] = T(1) - sum;
+    }
+    if (!ok) continue;
+    bool feasible = true;
+    for (int a = 0; a < k; ++a) feasible = feasible && !(lam[a] < zero);
+    if (!feasible) continue;
+    vec3<T> p = p0 * lam[0];
+    for (int a = 1; a < k; ++a) p = p + s.v[idx[a]].p * lam[a];
+    const T d2 = k == 4 ? zero : dot(p, p);  // a feasible tetrahedron holds the origin
+    if (d2 < best || (d2 == best && k < best_k)) {
+      best = d2;
+      best_mask = mask;
+      best_k = k;
+      best_v = k == 4 ? vec3<T>{zero, zero, zero} : p;
+    }
+  }
+  Sx<T> q;
+  q.n = 0;
+  for (int j = 0; j < n; ++j)
+    if (best_mask & (1 << j)) q.v[q.n++] = s.v[j];
+  s = q;
+  v = best_v;
+}
+
 // one iteration with the exact supports xa (body 1 along -v) and xb (body 2 along v)
 template <class Bodies, class T>
 OGX_HD void refine_step(const Bodies& B, RefineStateT<T>& r, int xa, int xb) {
@@ -981,10 +1089,22 @@ OGX_HD void refine_step(const Bodies& B, RefineStateT<T>& r, int xa, int xb) {
   r.ib[s.n] = xb;
   s.n++;
   Unc u{false};
+  const Sx<T> grown = s;
   subdistance(s, r.v, u);
   r.lam_valid = false;
   if (s.n != 4 && !(dot(r.v, r.v) < vv * T(1.0 - 1e-12))) {
-    // no progress: a tie support spanning a degenerate simplex -- keep the last answer
+    // the region decisions made no progress although the gap says progress is possible:
+    // solve the step again by exhaustive search
+    Sx<T> t = grown;
+    vec3<T> vt;
+    closest_exhaustive(t, vt);
+    if (t.n == 4 || dot(vt, vt) < vv * T(1.0 - 1e-12)) {
+      s = t;
+      r.v = vt;
+    }
+  }
+  if (s.n != 4 && !(dot(r.v, r.v) < vv * T(1.0 - 1e-12))) {
+    // still none: a tie support spanning a degenerate simplex -- keep the last answer
     s = prev;
     r.v = vprev;
     for (int j = 0; j < s.n; ++j) {

@@ -4,22 +4,31 @@
 namespace ogx {
 
 // ---------------------------------------------------------------------------------
+// Packs every body and marks the ones with a NaN or infinite coordinate in the body
+// table (point count stored negated, see body_points), which the binning turns into
+// OGX_PAIR_BAD_INPUT for their pairs; a later upload of finite points clears the mark.
 __global__ void k_pack(const float* __restrict__ aos, const int64_t* __restrict__ voff,
-                       const BodyRef* __restrict__ bodies, int nbodies, float* __restrict__ pool) {
+                       BodyRef* __restrict__ bodies, int nbodies, float* __restrict__ pool) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int b = warp; b < nbodies; b += nwarps) {
     const BodyRef r = bodies[b];
-    const int n4 = round4(r.n);
+    const int n = body_points(r);
+    const int n4 = round4(n);
     const float* src = aos + 3 * voff[b];
     float* dst = pool + 4 * (size_t)r.quad;
+    bool finite = true;
     for (int i = lane; i < n4; i += 32) {
-      const int s = i < r.n ? i : 0;
-      dst[i] = src[3 * s];
-      dst[n4 + i] = src[3 * s + 1];
-      dst[2 * n4 + i] = src[3 * s + 2];
+      const int s = i < n ? i : 0;
+      const float x = src[3 * s], y = src[3 * s + 1], z = src[3 * s + 2];
+      finite = finite && is_finite(x) && is_finite(y) && is_finite(z);
+      dst[i] = x;
+      dst[n4 + i] = y;
+      dst[2 * n4 + i] = z;
     }
+    finite = __all_sync(0xffffffffu, finite);
+    if (lane == 0) bodies[b].n = finite ? n : -n;
   }
 }
 
@@ -58,9 +67,9 @@ __global__ void k_bin(DevBatch B) {
         const gkSimplex& s = B.smp[p];
         work = s.nvrtx == 4 || !(B.dist[p] > FLT_EPSILON);
         if (!work) {
-          const fv3 w0 = v3<float>(s.witnesses[0][0], s.witnesses[0][1], s.witnesses[0][2]);
-          const fv3 w1 = v3<float>(s.witnesses[1][0], s.witnesses[1][1], s.witnesses[1][2]);
-          store3(B.nrm + 3 * (size_t)p, unit_or_x(w1 - w0));
+          MemBodies mb;
+          mb.bind(B.pool, B.bodies[pr.x], B.bodies[pr.y]);
+          store3(B.nrm + 3 * (size_t)p, simplex_sep_normal(mb, s));
           if (B.status) B.status[p] = 0;
         }
       } else {
@@ -98,7 +107,7 @@ __device__ void refine_store(const DevBatch& B, int p, const BodyRef& ra, const 
       const int q = atomicAdd(B.counts + kCntSpillLate, 1);
       B.spill[B.npairs - 1 - q] = p | kSpill64;
     } else {
-      store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
+      store3(B.nrm + 3 * (size_t)p, sep_normal(g));
     }
   }
 }
@@ -252,7 +261,7 @@ __global__ void __launch_bounds__(128) k_polish(DevBatch B) {
 }
 
 
-cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
+cudaError_t launch_pack(const float* aos, const int64_t* voff, BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st) {
   k_pack<<<grid, 256, 0, st>>>(aos, voff, bodies, nbodies, pool);
   return cudaGetLastError();

@@ -170,7 +170,7 @@ __device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, 
     store_simplex(B.smp + p, g);
     B.dist[p] = g.dist;
     if (B.status) B.status[p] = g.status;
-    if (B.mode == kModeGjkEpa && !contact && !g.polish) store3(B.nrm + 3 * (size_t)p, unit_or_x(g.w1 - g.w0));
+    if (B.mode == kModeGjkEpa && !contact && !g.polish) store3(B.nrm + 3 * (size_t)p, sep_normal(g));
     // pairs sent to the FP64 refinement get their normal there
   }
   const bool to_epa = lead && B.mode == kModeGjkEpa && contact;
@@ -325,7 +325,7 @@ cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream
 cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st, bool late = false);
 cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);
-cudaError_t launch_pack(const float* aos, const int64_t* voff, const BodyRef* bodies, int nbodies,
+cudaError_t launch_pack(const float* aos, const int64_t* voff, BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st);
 cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st);
 cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st);

@@ -101,7 +101,11 @@ ogx_status setup(int dev, Setup** out) {
     if (!g || !q) return ogx_fail(OGX_ERR_CUDA, "no kernel variant for bucket %d", b);
     s.gjk[b] = *g;
     s.epa[b] = *q;
-    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * sizeof(EpaMemSmall);  // < 48 KB
+    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * sizeof(EpaMemSmall);
+    // launches here take no dynamic shared memory beyond the default 48 KB per block
+    if (s.smem_epa[b] > 48 * 1024)
+      return ogx_fail(OGX_ERR_CUDA, "EPA variant for bucket %d needs %zu B of shared memory (> 48 KB)", b,
+                      s.smem_epa[b]);
     int per = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, g->fn, kNoAllocBlock, 0);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "occupancy");

@@ -61,7 +61,7 @@ __global__ void k_transform(const float* __restrict__ local, const BodyRef* __re
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int b = warp; b < nbodies; b += nwarps) {
     const BodyRef r = bodies[b];
-    const int n4 = round4(r.n);
+    const int n4 = round4(body_points(r));
     const size_t base = 4 * (size_t)r.quad;
     const float* m = xf + 12 * (size_t)b;
     const double r00 = m[0], r01 = m[1], r02 = m[2], r10 = m[3], r11 = m[4], r12 = m[5];
@@ -596,8 +596,19 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
 extern "C" ogx_status ogx_server_destroy(ogx_server* S) {
   if (!S) return OGX_OK;
   {
-    std::lock_guard<std::mutex> lk(S->mu);
+    std::unique_lock<std::mutex> lk(S->mu);
     S->stop = true;
+    // a transform upload copies into a ring slot's staging and launches into its device
+    // buffer without the lock: wait until none is under way before anything is freed
+    auto writing = [&] {
+      for (char c : S->world_writing)
+        if (c) return true;
+      return false;
+    };
+    const auto deadline = Clock::now() + std::chrono::seconds(10);
+    while (writing())
+      if (S->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && writing())
+        return ogx_fail(OGX_ERR_BUSY, "a transform upload is still running after 10 s; server stopped, not freed");
   }
   S->cv_work.notify_all();
   if (S->sched.joinable()) S->sched.join();
@@ -611,7 +622,16 @@ extern "C" ogx_status ogx_server_destroy(ogx_server* S) {
 
 extern "C" ogx_status ogx_server_set_transforms(ogx_server* S, const float* xf, int64_t* version) {
   if (!S || !xf || !version) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
+  // a pose with a NaN or an infinity would put non-finite points into the world copy
+  // that every request of the version reads: refuse the update
+  {
+    const size_t nf = 12 * (size_t)S->local->nbodies;
+    for (size_t i = 0; i < nf; ++i)
+      if (!ogx::is_finite(xf[i]))
+        return ogx_fail(OGX_ERR_INVALID, "pose of body %zu has a NaN or infinite entry", i / 12);
+  }
   std::unique_lock<std::mutex> lk(S->mu);
+  if (S->stop) return ogx_fail(OGX_ERR_INVALID, "server is being destroyed");
   // the next version's ring slot must not be read by a request in flight or queued, nor
   // be written by another upload (another caller may take that version meanwhile)
   auto in_use = [&](int w) {

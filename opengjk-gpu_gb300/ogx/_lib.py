@@ -22,6 +22,7 @@ ERRORS = {
     -6: "OGX_ERR_BUSY",
 }
 ERR_BUSY = -6
+ERR_CAPACITY = -5
 
 FLAG_FP64_ESCALATE = 1
 FLAG_FP64_POLISH = 2

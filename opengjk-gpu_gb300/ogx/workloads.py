@@ -155,8 +155,9 @@ def _place_pairs(rng, pts64: np.ndarray, counts: np.ndarray, offsets: np.ndarray
     return pts64
 
 
-def plain(seed: int = 1, n_pairs: int = 1000, n_verts: int = 32) -> Batch:
-    """32 points uniform on the unit sphere x r ~ U[0.5, 2] + c ~ U[-5, 5]^3."""
+def plain(seed: int = 1, n_pairs: int = 1000, n_verts: int = 32, dtype=np.float32) -> Batch:
+    """32 points uniform on the unit sphere x r ~ U[0.5, 2] + c ~ U[-5, 5]^3 (float32
+    coordinates; dtype=np.float64 keeps them in double, the inputs of FP64 callers)."""
     rng = np.random.default_rng(seed)
     nb = 2 * n_pairs
     counts = np.full(nb, n_verts, dtype=np.int32)
@@ -165,7 +166,7 @@ def plain(seed: int = 1, n_pairs: int = 1000, n_verts: int = 32) -> Batch:
     u = _unit_vectors(rng, nb * n_verts).reshape(nb, n_verts, 3)
     pts = (u * r[:, None, None] + c[:, None, :]).reshape(-1, 3)
     pairs = np.arange(nb, dtype=np.int32).reshape(-1, 2)
-    return Batch(pts.astype(np.float32), _offsets(counts), counts, pairs, "plain",
+    return Batch(pts.astype(dtype), _offsets(counts), counts, pairs, "plain",
                  {"n_verts": n_verts})
 
 

@@ -55,8 +55,14 @@ def build(force: bool = False) -> None:
         subprocess.run(["make", "-s", "-C", HERE, "liborc.so"], check=True)
 
 
-def build_ref(ref_dir: str = "/root/reference") -> bool:
+def reference_dir() -> str:
+    """The reference checkout: $REFERENCE_DIR, else a sibling of this repository."""
+    return os.environ.get("REFERENCE_DIR", os.path.normpath(os.path.join(HERE, "..", "..", "reference")))
+
+
+def build_ref(ref_dir: str | None = None) -> bool:
     """Compile the reference's own CPU GJK/EPA into oracle/_ref (validation only)."""
+    ref_dir = ref_dir or reference_dir()
     if not os.path.isdir(os.path.join(ref_dir, "GJK", "cpu")):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={ref_dir}"], check=True)
@@ -93,10 +99,14 @@ def run(coords, offsets, counts, pairs, *, mode=MODE_GJK_EPA, precision="f64", t
 
     coords: (P, 3) float32 points of all bodies; offsets/counts: first point and
     point count per body; pairs: (N, 2) body indices.  precision "f64" widens the
-    FP32 coordinates exactly to double (the parity oracle); "f32" is the reference's
+    FP32 coordinates exactly to double (the parity oracle); float64 coordinates given
+    with "f64" are used as they are (inputs of FP64 callers); "f32" is the reference's
     shipped precision.  Zero tolerances select the reference constants.
     """
     lib = _load()
+    given64 = precision == "f64" and np.asarray(coords).dtype == np.float64
+    if given64:
+        c64 = np.ascontiguousarray(coords, dtype=np.float64).reshape(-1, 3)
     coords = np.ascontiguousarray(coords, dtype=np.float32).reshape(-1, 3)
     offsets = np.ascontiguousarray(offsets, dtype=np.int64)
     counts = np.ascontiguousarray(counts, dtype=np.int32)
@@ -106,7 +116,7 @@ def run(coords, offsets, counts, pairs, *, mode=MODE_GJK_EPA, precision="f64", t
         results = np.zeros(n, dtype=RESULT_DTYPE)
     cfg = _Config(eps_rel, eps_tot, gjk_max_iter, epa_tol, epa_max_iter)
     if precision == "f64":
-        c = coords.astype(np.float64)
+        c = c64 if given64 else coords.astype(np.float64)
         fn = lib.orc_run_f64
     elif precision == "f32":
         c = coords

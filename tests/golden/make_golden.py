@@ -23,7 +23,7 @@ sys.path.insert(0, os.path.join(ROOT, "opengjk-gpu_gb300"))
 from ogx import workloads as W  # noqa: E402
 from oracle import orc  # noqa: E402
 
-REF = os.environ.get("REFERENCE_DIR", "/root/reference")
+REF = os.environ.get("REFERENCE_DIR", os.path.normpath(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference")))
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

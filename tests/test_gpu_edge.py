@@ -9,6 +9,9 @@ from ogx import workloads as W
 
 pytestmark = pytest.mark.gpu
 
+# agreement of separated-pair normals between a fused GJK+EPA call and GJK then EPA-only
+SEP_NORMAL_AGREE = 1e-5
+
 
 def test_empty_batch(engine):
     import torch
@@ -113,7 +116,10 @@ def test_epa_only_matches_fused(engine):
     engine.run(ctx, pool, pairs, engine.MODE_EPA, out=r)
     sep = r.to_host()
     assert np.array_equal(fused["dist"], sep["dist"])
-    assert np.allclose(fused["normal"], sep["normal"], atol=1e-6)
+    # contacts run the same EPA; a separated pair's normal comes from the GJK pass's own
+    # closest point in the fused call and is re-solved from the stored simplex in the
+    # EPA-only call: the two agree to that point's FP32 accuracy (a few 1e-6)
+    assert np.allclose(fused["normal"], sep["normal"], atol=SEP_NORMAL_AGREE)
 
 
 def test_reference_tolerance_mode(engine, orc):
@@ -243,3 +249,46 @@ def test_stage_timeline(engine):
     assert set(tl) == names, sorted(tl)
     assert all(0.0 <= v <= tl["end"] + 1e-3 for v in tl.values()), tl
     assert tl["refine"] <= tl["epa_late"] + 1e-3
+
+
+def test_non_finite_coordinates_flagged(engine):
+    """A body with a NaN or an infinite coordinate makes its pairs bad input -- status
+    OGX_PAIR_BAD_INPUT, distance NaN, normal (1,0,0), simplex with no vertex -- through the
+    engine, the streamed call and the reference-compatible API; every other pair's results
+    are those of the same batch with finite points, and an upload of finite points clears
+    the mark.  (The reference checks no input; a non-finite point there gives undefined
+    results.)"""
+    import torch
+    from ogx import _lib, refapi
+    b = W.ellipsoid(seed=45, n_pairs=600)
+    coords = b.coords.copy()
+    coords[b.offsets[3] + 1, 0] = np.nan
+    coords[b.offsets[10], 2] = np.inf
+    coords[b.offsets[401] + b.counts[401] - 1, 1] = -np.inf
+    flagged = np.isin(b.pairs, [3, 10, 401]).any(axis=1)
+    assert flagged.sum() == 3
+    bad = W.Batch(coords, b.offsets, b.counts, b.pairs, "non-finite")
+    ref = engine.query(b, engine.MODE_GJK_EPA)
+
+    def check(got, with_status=True):
+        if with_status:
+            assert np.all(got["status"][flagged] & _lib.PAIR_BAD_INPUT)
+            assert not np.any(got["status"][~flagged] & _lib.PAIR_BAD_INPUT)
+            assert np.all(got["simplex"]["nvrtx"][flagged] == 0)
+        assert np.isnan(got["dist"][flagged]).all()
+        assert np.array_equal(got["normal"][flagged], np.tile(np.float32([1, 0, 0]), (3, 1)))
+        assert np.array_equal(got["dist"][~flagged], ref["dist"][~flagged])
+        assert np.array_equal(got["normal"][~flagged], ref["normal"][~flagged])
+
+    check(engine.query(bad, engine.MODE_GJK_EPA))
+    ctx = engine.Context(0)
+    pool = engine.Pool(ctx, b.counts)
+    check(engine.streamed(ctx, pool, torch.from_numpy(coords).pin_memory(), np.ascontiguousarray(b.pairs)))
+    pool.upload(b.coords)  # finite points again: nothing flagged
+    again = engine.run(ctx, pool, torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()).to_host()
+    ctx.synchronize()
+    assert np.array_equal(again["dist"], ref["dist"]) and not np.any(again["status"] & _lib.PAIR_BAD_INPUT)
+    bd1, bd2, _ = refapi.from_batch(bad)
+    smp, dist, nrm = refapi.compute_gjk_epa(bd1, bd2)
+    check({"dist": dist, "normal": nrm, "simplex": smp}, with_status=False)
+    assert np.all(smp["nvrtx"][flagged] == 0)

@@ -51,11 +51,12 @@ def certify_witnesses(b, res, o):
     out["contacts"] = int(c.size)
     out["contact_inconsistent"] = int(np.sum(incons > ABS4 * np.maximum(1.0, depth)))
     out["contact_off_support"] = int(np.sum((np.abs(ga) > ABS4) | (np.abs(gb) > ABS4)))
-    # separated pairs outside the contact band; the distance vector is the oracle's (FP32
-    # witnesses of a tiny distance do not resolve its direction)
+    # separated pairs outside the contact band; the distance vector's direction is the
+    # engine's normal (computed from the closest point -v itself, so it resolves tiny
+    # distances, which the difference of two FP32 witnesses does not)
     band = np.abs(o["dist"]) <= parity.BAND * parity.pair_scale(b)
     s = np.flatnonzero(~col & ~band & (o["epa_exit"] <= 0))
-    dirn = o["wit"][s, 1] - o["wit"][s, 0]
+    dirn = res["normal"][s].astype(np.float64)
     dirn /= np.maximum(np.linalg.norm(dirn, axis=1, keepdims=True), 1e-300)
     length = np.abs(np.linalg.norm(w[s, 1] - w[s, 0], axis=1) - d[s])
     hi, lo = support_extremes(b, s, dirn)
@@ -70,7 +71,7 @@ def certify_witnesses(b, res, o):
 @pytest.mark.parametrize("name", ["powerlaw_1M", "ellipsoid_100k"])
 def test_full_size_parity(engine, orc, name):
     if name == "powerlaw_1M":
-        b = W.powerlaw(seed=3, n_pairs=1_000_000)
+        b = W.powerlaw(seed=1000, n_pairs=1_000_000)  # the benchmark's own batch
     else:
         b = W.ellipsoid(seed=2, n_pairs=100_000)
     res = engine.query(b, engine.MODE_GJK_EPA)
@@ -79,6 +80,12 @@ def test_full_size_parity(engine, orc, name):
     rep = parity.check(b, res, o, label=name, witness_sample=5000)
     cert = certify_witnesses(b, res, o)
     print(f"\n{name}: {rep}\n{name} witnesses: {cert}")
+    out_dir = os.environ.get("OGX_PARITY_REPORT_DIR")
+    if out_dir:  # the report of this run, for the measurement summaries
+        import json
+        os.makedirs(out_dir, exist_ok=True)
+        with open(os.path.join(out_dir, f"parity_{name}.json"), "w") as f:
+            json.dump({"workload": name, "report": rep, "witness_certificates": cert}, f, indent=1)
     parity.assert_parity(rep, max_witness_mismatch_frac=2e-3)
     assert cert["contact_inconsistent"] == 0 and cert["contact_off_support"] == 0, cert
     assert cert["sep_length_off"] == 0 and cert["sep_off_support"] == 0, cert

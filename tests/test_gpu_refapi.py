@@ -8,6 +8,10 @@ from ogx import refapi, workloads as W
 
 pytestmark = pytest.mark.gpu
 
+# agreement of separated-pair normals between a fused GJK+EPA call and GJK then EPA-only
+# (the fused call uses its GJK closest point, EPA-only re-solves it from the simplex)
+SEP_NORMAL_AGREE = 1e-5
+
 
 def _res(smp, dist, nrm, status_contact):
     return {"dist": dist, "simplex": smp, "normal": nrm, "status": status_contact}
@@ -35,10 +39,12 @@ def test_distances_then_epa_matches_fused(engine):
     nrm = refapi.compute_epa(bd1, bd2, smp, dist)
     smp2, dist2, nrm2 = refapi.compute_gjk_epa(bd1, bd2)
     assert np.array_equal(dist, dist2)
-    assert np.allclose(nrm, nrm2, atol=1e-6)
+    # separated normals: the fused call's from its GJK closest point, the EPA-only call's
+    # re-solved from the simplex (they agree to that point's FP32 accuracy)
+    assert np.allclose(nrm, nrm2, atol=SEP_NORMAL_AGREE)
     w1, w2, n3 = refapi.compute_collision_information(bd1, bd2, smp.copy(), dist.copy())
     assert np.allclose(w1, smp2["witnesses"][:, 0], atol=1e-6)
-    assert np.allclose(n3, nrm2, atol=1e-6)
+    assert np.allclose(n3, nrm2, atol=SEP_NORMAL_AGREE)
 
 
 def test_indexed_matches_pairwise(engine):
@@ -95,7 +101,7 @@ def test_device_api(engine):
                                                 P(d_smp.data_ptr()), P(d_dist.data_ptr()), P(d_nrm.data_ptr())))
     eng = engine.query(b, engine.MODE_GJK_EPA)
     assert np.array_equal(d_dist.cpu().numpy(), eng["dist"])
-    assert np.allclose(d_nrm.cpu().numpy(), eng["normal"], atol=1e-6)
+    assert np.allclose(d_nrm.cpu().numpy(), eng["normal"], atol=SEP_NORMAL_AGREE)
     # bd1 / bd2 descriptor arrays in device memory
     d1 = torch.from_numpy(desc[b.pairs[:, 0]].view(np.uint8).copy()).cuda()
     d2 = torch.from_numpy(desc[b.pairs[:, 1]].view(np.uint8).copy()).cuda()

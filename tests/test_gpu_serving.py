@@ -98,6 +98,79 @@ def test_warm_start_parity(scene, orc):
             parity.assert_parity(rep, max_witness_mismatch_frac=2e-3)
 
 
+def _agree(b, a, m):
+    """Two engine results of one request agree within the parity tolerances: the same
+    verdict outside the contact band, separated distances within 2 REL relative, depths
+    within 2 ABS4 (each is within one tolerance of the oracle)."""
+    s = parity.pair_scale(b)
+    da, dm = a["dist"].astype(np.float64), m["dist"].astype(np.float64)
+    band = np.minimum(np.abs(da), np.abs(dm)) <= 2 * parity.BAND * s
+    ca, cm = (a["status"] & 8) != 0, (m["status"] & 8) != 0
+    assert np.all((ca == cm) | band)
+    sep = ~ca & ~cm & ~band
+    assert np.all(np.abs(da[sep] - dm[sep]) <= 2 * parity.REL * np.abs(da[sep]))
+    con = ca & cm & ~band
+    assert np.all(np.abs(da[con] - dm[con]) <= 2 * parity.ABS4)
+
+
+def _copy(req):
+    return {k: v.copy() for k, v in req.results().items()}
+
+
+def test_warm_start_mix_parity(scene, orc):
+    """Continuous batching with warm starts on, as the serving benchmark runs: more
+    requests than slots, ticks that share most body pairs, so requests read and write the
+    shared warm-start table while others run.  A request's starting simplex then depends on
+    what ran before it, so alone and mixed results need not be bit-identical; each must
+    meet every parity rule against the FP64 oracle, and the two runs of a request must agree
+    within the stated tolerances."""
+    rng = np.random.default_rng(12)
+    ticks = [20, 21, 22, 23]
+    kw = dict(warm_start=True, slots=2, slot_pairs=20000, max_pairs_in_flight=30000)
+    jobs = []
+    for t in ticks:
+        for n in (3000, 9000, 16000):
+            jobs.append((t, scene.candidate_pairs(t, n)[rng.permutation(n)]))
+    with _server(scene, **kw) as srv:
+        vers = {t: srv.set_transforms(scene.transforms(t)) for t in ticks}
+        alone = [_copy(srv.wait(srv.submit(vers[t], p))) for t, p in jobs]
+    with _server(scene, **kw) as srv:
+        vers = {t: srv.set_transforms(scene.transforms(t)) for t in ticks}
+        reqs = [srv.submit(vers[t], p) for t, p in jobs]
+        mixed = [_copy(srv.wait(r)) for r in reqs]
+    with _server(scene, **dict(kw, warm_start=False)) as srv:
+        vers = {t: srv.set_transforms(scene.transforms(t)) for t in ticks}
+        cold = [_copy(srv.wait(srv.submit(vers[t], p))) for t, p in jobs]
+    warm_hits = 0
+    for (t, pairs), a, m, c in zip(jobs, alone, mixed, cold):
+        b = _batch(scene, scene.world(scene.transforms(t)), pairs)
+        o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=16)
+        for res, label in ((a, "alone"), (m, "mixed")):
+            parity.assert_parity(parity.check(b, res, o, label=f"tick{t}-{len(pairs)}-{label}"),
+                                 max_witness_mismatch_frac=2e-3)
+        _agree(b, a, m)
+        warm_hits += int(np.sum(a["dist"] != c["dist"]))
+    # the warm starts did change starting points (results differ in their last bits from
+    # the cold run somewhere), so the mix above really shared the warm-start table
+    assert warm_hits > 0
+
+
+def test_wait_timeout_returns_busy(scene):
+    """A wait whose host-side time limit runs out before the request is done returns
+    OGX_ERR_BUSY and leaves the request registered; a later wait collects its results."""
+    from ogx import _lib
+    pairs = scene.candidate_pairs(8, 60000)
+    with _server(scene, warm_start=False) as srv:
+        v = srv.set_transforms(scene.transforms(8))
+        req = srv.submit(v, pairs)
+        with pytest.raises(_lib.OgxError) as ei:
+            srv.wait(req, timeout_s=1e-6)
+        assert ei.value.status == _lib.ERR_BUSY
+        assert not req.done
+        srv.wait(req, timeout_s=60.0)
+        assert req.done and np.isfinite(req.dist).all()
+
+
 def test_admission_limits(scene):
     from ogx import _lib
     with _server(scene, warm_start=False, slots=1, slot_pairs=1000, max_pairs_in_flight=1000,
@@ -199,3 +272,23 @@ def test_concurrent_transform_uploads(scene, engine):
             req = srv.wait(srv.submit(vers[t], pairs))
             ref = engine.query(_batch(scene, scene.world(scene.transforms(t)), pairs), engine.MODE_GJK_EPA)
             assert np.array_equal(req.dist, ref["dist"]), t
+
+
+def test_non_finite_pose_refused(scene):
+    """A pose update holding a NaN or an infinity is refused (it would put non-finite
+    points into the world copy every request of the version reads); the server keeps
+    working with the versions it has."""
+    from ogx import _lib
+    with _server(scene, warm_start=False) as srv:
+        v = srv.set_transforms(scene.transforms(1))
+        xf = scene.transforms(2)
+        xf[17, 4] = np.nan
+        with pytest.raises(_lib.OgxError) as ei:
+            srv.set_transforms(xf)
+        assert ei.value.status == -1 and "body 17" in str(ei.value)
+        xf[17, 4] = 0.0
+        xf[5, 10] = np.inf
+        with pytest.raises(_lib.OgxError):
+            srv.set_transforms(xf)
+        req = srv.wait(srv.submit(v, scene.candidate_pairs(1, 500)))
+        assert np.isfinite(req.dist).all()

@@ -89,7 +89,7 @@ void one(const Job& J, int i, Work& M) {
       st |= o.status;
       ei = o.iters;
     } else {
-      n = unit_or_x(w1 - w0);
+      n = sep_normal(g);
     }
   }
   J.dist[i] = d;
