@@ -56,7 +56,9 @@ typedef struct ogx_config {
   float epa_vis;      /* face visibility threshold relative to the polytope scale */
   int epa_max_iter;   /* EPA iteration cap (reference: 64) */
   int flags;          /* OGX_FLAG_* */
-  float polish_rel;   /* FP64 re-solve when the FP32 distance bound exceeds this */
+  float polish_rel;   /* >= 0; no longer read: with OGX_FLAG_FP64_POLISH every separated
+                       * pair's final simplex is certified and re-solved, or continued, in
+                       * FP64 (the field keeps the structure's layout) */
 } ogx_config;
 
 #define OGX_FLAG_FP64_ESCALATE 1 /* near-degenerate steps re-run in FP64 */

@@ -272,11 +272,13 @@ OGX_HD int tri_weights(fv3 p0, fv3 p1, fv3 p2, float* l) {
 // contact is split into coplanar triangles), the neighbour that holds the projection is
 // used, so that w0 - w1 = depth * normal holds.
 template <class Mem, class Bodies>
-// With report_closer, returns true when a neighbour of the closest face is closer than it
-// in FP64 (the FP32 planes ranked the two wrongly): nothing is emitted then and the
-// caller runs the contact again with FP64 planes; without, the closest face's own result
-// is emitted in that case.
-OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o, bool report_closer) {
+// With rerun_ok, returns true when the origin's projection leaves the closest face
+// towards a neighbour that is not coplanar with it in FP64: nothing is emitted then and
+// the caller runs the contact again with FP64 planes.  Without (the FP64-plane pass
+// itself, whose closest face is picked on the planes rounded to float, so two faces a
+// rounding apart can swap), the result comes from that near-coplanar neighbour, which
+// holds the projection.
+OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o, bool rerun_ok) {
   int a = M.fv[f][0], b = M.fv[f][1], c = M.fv[f][2];
   float l[3];
   for (int hop = 0; hop < 4; ++hop) {
@@ -293,11 +295,11 @@ OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o,
                       (nf.x * ng.x + nf.y * ng.y + nf.z * ng.z) > 1.0f - 1e-5f;
     if (!near) break;
     // In exact arithmetic the origin projects into the closest face of the convex
-    // polytope, so the neighbour it leaves through is either coplanar with it (a flat
-    // patch split into triangles: the witnesses come from the neighbour) or closer (the
-    // FP32 planes ranked the two wrongly).  Decided on FP64 planes of the exact points:
-    // a neighbour that is neither -- a few 1e-5 off, on dense flat patches -- is not a
-    // supporting plane, and the projection leaves the closest face by rounding only.
+    // polytope, so a neighbour it leaves through is coplanar with it (a flat patch split
+    // into triangles: the witnesses come from the neighbour).  Decided on FP64 planes of
+    // the exact points; a neighbour that is not -- FP32 planes made the polytope a little
+    // non-convex or ranked the faces wrongly, on dense flat patches -- would give a normal
+    // a few 1e-5 off and witnesses off the normal: the contact runs again on FP64 planes.
     const double4 pf = face_plane64(M, B, f), pg = face_plane64(M, B, g2);
     const double dn = ::fabs(pf.x - pg.x) + ::fabs(pf.y - pg.y) + ::fabs(pf.z - pg.z);
     const double sc = ::fmax(1.0, ::fabs(pf.w));
@@ -305,8 +307,8 @@ OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o,
       f = g2;
       continue;
     }
-    if (report_closer && pg.w < pf.w - 1e-12 * sc) return true;
-    break;
+    if (rerun_ok) return true;
+    f = g2;
   }
   const int2 ia = M.vid[a], ib = M.vid[b], ic = M.vid[c];
   o.w0 = B.point(0, ia.x) * l[0] + B.point(0, ib.x) * l[1] + B.point(0, ic.x) * l[2];

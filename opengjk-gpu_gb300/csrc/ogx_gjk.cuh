@@ -17,9 +17,9 @@
 //    on the exact Minkowski points re-read from the pool (OGX_F_FP64_ESCALATE).
 //  * Termination also stops when the support pair is already in the simplex (no
 //    progress is possible) and when the gap is below FP32 rounding of |v| |w|.
-//  * The final simplex can be re-solved in FP64 (exact closest point of the final
-//    feature) when the FP32 distance is not known to polish_rel (OGX_F_FP64_POLISH);
-//    on the device that runs as a separate pass over the pairs that need it.
+//  * The final simplex of a separated pair is re-solved in FP64 (exact closest point of
+//    the final feature, certified by an exact support check, else GJK continues in FP64;
+//    OGX_F_FP64_POLISH); on the device that runs as a separate pass.
 #pragma once
 
 #include "ogx_common.cuh"
@@ -448,7 +448,7 @@ struct GjkState {
   int iters;
   int status;
   int exit;     // why the loop ended (GJK_EXIT_*)
-  bool polish;  // the FP32 distance is not known to polish_rel: re-solve in FP64
+  bool polish;  // separated: certify and re-solve (or continue) in FP64
   int wa, wb;   // support pair along the final direction
   bool certain; // that support is the exact (FP64) support along the exact direction
 };
@@ -775,10 +775,11 @@ OGX_HD void gjk_end(const Team& t, const Bodies& B, const Config& cfg, const Gjk
   g.wa = ia;
   g.wb = ib;
   if ((cfg.flags & OGX_F_FP64_POLISH) && g.n >= 1 && g.n <= 3 && !gjk_contact(g)) {
-    const float errb = 16.0f * FLT_EPSILON * sqrtf(g.wmax2);
-    // a pair that ran into the iteration cap did not converge (the region decisions can
-    // cycle): its FP64 continuation decides it
-    g.polish = (g.n >= 2 && errb > cfg.polish_rel * g.dist) || g.exit == GJK_EXIT_CAP;
+    // Every separated pair is certified or continued in FP64: a stop on the FP32 gap
+    // bounds the distance (about 1e-7 relative) but not its direction, which on flat
+    // closest features can stay ~1e-4 off until the exact feature is found; a pair that
+    // ran into the iteration cap has not converged at all (the region decisions can cycle).
+    g.polish = true;
   }
   if (g.polish) {
     // Is the exact support along the exact closest point v64 one of the final simplex's
