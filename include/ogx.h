@@ -198,6 +198,19 @@ ogx_status ogx_broad_create(ogx_ctx* ctx, int max_bodies, ogx_broad** out);
 ogx_status ogx_broadphase(ogx_broad* broad, const ogx_pool* pool, float cell, float margin,
                           int max_pairs, gkCollisionPair* d_pairs, int* d_result);
 ogx_status ogx_broad_destroy(ogx_broad* broad);
+/* Candidate pairs with the reference's own broad-phase semantics
+ * (visualization/integrate_final_gjk.cu:467-570: insert_objects_kernel /
+ * count_pairs_kernel / generate_pairs_kernel): d_spheres[num_bodies] = float4 (x, y, z,
+ * bounding radius); each sphere belongs to the grid cell of its centre,
+ * floor((p + boundary) / cell) per axis clamped to [0, grid_size); pairs (i, j > i) are
+ * the spheres in i's 27 neighbouring cells with fx*fx + fy*fy + fz*fz < (r_i + r_j)^2 in
+ * FP32.  The pairs are written sorted by (i, j); d_result[0] = pairs found (may exceed
+ * max_pairs: the first max_pairs are written), d_result[1] = 0.  The reference caps the
+ * bodies stored per cell and drops the rest in an atomic-dependent order; this mode has
+ * no such cap, so the pair sets are equal wherever no reference cell overflows. */
+ogx_status ogx_broadphase_spheres(ogx_broad* broad, const float* d_spheres, int num_bodies, float cell,
+                                  float boundary, int grid_size, int max_pairs, gkCollisionPair* d_pairs,
+                                  int* d_result);
 
 /* GJK then EPA from host memory to host memory in one call, with the transfers
  * overlapped with the kernels: the pool's points (xyz of all bodies, concatenated, as

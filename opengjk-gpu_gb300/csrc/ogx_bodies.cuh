@@ -14,6 +14,42 @@
 
 namespace ogx {
 
+// The support values of a block of 4 points (x, y, z planes) along d: sdot() of each
+// point.  On the device two points at a time with the packed FP32 instructions of this
+// architecture: a multiply and two fused multiply-adds round exactly as sdot()'s, in half
+// the instructions.
+OGX_HD void sdot4(const float4& x, const float4& y, const float4& z, fv3 d, float* v) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  const float2 dx = make_float2(d.x, d.x), dy = make_float2(d.y, d.y), dz = make_float2(d.z, d.z);
+  const float2 a = __ffma2_rn(make_float2(z.x, z.y), dz,
+                              __ffma2_rn(make_float2(y.x, y.y), dy, __fmul2_rn(make_float2(x.x, x.y), dx)));
+  const float2 b = __ffma2_rn(make_float2(z.z, z.w), dz,
+                              __ffma2_rn(make_float2(y.z, y.w), dy, __fmul2_rn(make_float2(x.z, x.w), dx)));
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+  v[3] = b.y;
+#else
+  v[0] = sdot(x.x, y.x, z.x, d);
+  v[1] = sdot(x.y, y.y, z.y, d);
+  v[2] = sdot(x.z, y.z, z.z, d);
+  v[3] = sdot(x.w, y.w, z.w, d);
+#endif
+}
+
+// Fold a block of 4 support values (indices i0..i0+3) into the running (best, bi): the
+// block's maximum is compared once with the running best, and only a block that beats
+// it (strictly: an equal value keeps the earlier index) looks up which of its points
+// holds the maximum, the lowest first.  Same result as comparing point by point in index
+// order; NaN values never win.
+OGX_HD void block_best(const float* v, int i0, float& best, int& bi) {
+  const float m = fmaxf(fmaxf(v[0], v[1]), fmaxf(v[2], v[3]));
+  if (m > best) {
+    best = m;
+    bi = v[0] == m ? i0 : (v[1] == m ? i0 + 1 : (v[2] == m ? i0 + 2 : i0 + 3));
+  }
+}
+
 struct MemBodies {
   static constexpr bool kExact64 = false;  // dpoint() is the float point widened
   const float* base[2];  // x[0] of each body
@@ -77,23 +113,11 @@ struct MemBodies {
       const int q2 = q + Team::L;
       const float4 x = __ldg(X4 + q), y = __ldg(Y4 + q), z = __ldg(Z4 + q);
       const float4 x2 = __ldg(X4 + q2), y2 = __ldg(Y4 + q2), z2 = __ldg(Z4 + q2);
-      float v;
-      v = sdot(x.x, y.x, z.x, d);
-      if (v > best) { best = v; bi = 4 * q; }
-      v = sdot(x.y, y.y, z.y, d);
-      if (v > best) { best = v; bi = 4 * q + 1; }
-      v = sdot(x.z, y.z, z.z, d);
-      if (v > best) { best = v; bi = 4 * q + 2; }
-      v = sdot(x.w, y.w, z.w, d);
-      if (v > best) { best = v; bi = 4 * q + 3; }
-      v = sdot(x2.x, y2.x, z2.x, d);
-      if (v > best) { best = v; bi = 4 * q2; }
-      v = sdot(x2.y, y2.y, z2.y, d);
-      if (v > best) { best = v; bi = 4 * q2 + 1; }
-      v = sdot(x2.z, y2.z, z2.z, d);
-      if (v > best) { best = v; bi = 4 * q2 + 2; }
-      v = sdot(x2.w, y2.w, z2.w, d);
-      if (v > best) { best = v; bi = 4 * q2 + 3; }
+      float v[4], v2[4];
+      sdot4(x, y, z, d, v);
+      sdot4(x2, y2, z2, d, v2);
+      block_best(v, 4 * q, best, bi);
+      block_best(v2, 4 * q2, best, bi);
     }
 #endif
     for (; q < nb; q += Team::L) {
@@ -101,21 +125,14 @@ struct MemBodies {
       const float4 x = __ldg(reinterpret_cast<const float4*>(X) + q);
       const float4 y = __ldg(reinterpret_cast<const float4*>(Y) + q);
       const float4 z = __ldg(reinterpret_cast<const float4*>(Z) + q);
-      const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w},
-                  zs[4] = {z.x, z.y, z.z, z.w};
 #else
-      const float* xs = X + 4 * q;
-      const float* ys = Y + 4 * q;
-      const float* zs = Z + 4 * q;
+      const float4 x = make_float4_(X[4 * q], X[4 * q + 1], X[4 * q + 2], X[4 * q + 3]);
+      const float4 y = make_float4_(Y[4 * q], Y[4 * q + 1], Y[4 * q + 2], Y[4 * q + 3]);
+      const float4 z = make_float4_(Z[4 * q], Z[4 * q + 1], Z[4 * q + 2], Z[4 * q + 3]);
 #endif
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        const float v = sdot(xs[c], ys[c], zs[c], d);
-        if (v > best) {
-          best = v;
-          bi = 4 * q + c;
-        }
-      }
+      float v[4];
+      sdot4(x, y, z, d, v);
+      block_best(v, 4 * q, best, bi);
     }
   }
 };
@@ -190,17 +207,9 @@ struct RegBodies {
     bi = 0x7fffffff;
 #pragma unroll
     for (int j = 0; j < K; ++j) {
-      const int q4 = 4 * (t.lane() + j * L);
-      const float4 X = x[w][j], Y = y[w][j], Z = z[w][j];
-      float v;
-      v = sdot(X.x, Y.x, Z.x, d);
-      if (v > best) { best = v; bi = q4; }
-      v = sdot(X.y, Y.y, Z.y, d);
-      if (v > best) { best = v; bi = q4 + 1; }
-      v = sdot(X.z, Y.z, Z.z, d);
-      if (v > best) { best = v; bi = q4 + 2; }
-      v = sdot(X.w, Y.w, Z.w, d);
-      if (v > best) { best = v; bi = q4 + 3; }
+      float v[4];
+      sdot4(x[w][j], y[w][j], z[w][j], d, v);
+      block_best(v, 4 * (t.lane() + j * L), best, bi);
     }
   }
 };

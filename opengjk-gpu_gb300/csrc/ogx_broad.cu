@@ -273,6 +273,90 @@ static __global__ void k_sub_reduce(const int* __restrict__ off, int n, int cap,
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Bounding-sphere mode: the reference's own pair semantics (visualization/
+// integrate_final_gjk.cu:467-570).  Body b is a sphere (x, y, z, r); it lives in the one
+// grid cell of its centre, floor((p + boundary) / cell) per axis clamped to
+// [0, grid_size), and pairs (i, j > i) are the bodies in i's 27 neighbouring cells whose
+// spheres overlap: fx*fx + fy*fy + fz*fz < (r_i + r_j)^2, evaluated in FP32 in that order
+// (no fused multiply-add, as the reference builds its CUDA).  Pairs whose centres lie
+// more than one cell apart are not found even when the spheres overlap -- the
+// reference's behaviour, kept.  The reference stores at most a fixed number of bodies
+// per cell and drops the rest in an order set by atomics; the cells here have no such
+// capacity, so the pair sets agree whenever no reference cell overflows.
+
+__device__ __forceinline__ void sphere_cell(float4 s, float cell, float boundary, int grid, int& cx, int& cy,
+                                            int& cz) {
+  cx = min(max((int)floorf(__fdiv_rn(__fadd_rn(s.x, boundary), cell)), 0), grid - 1);
+  cy = min(max((int)floorf(__fdiv_rn(__fadd_rn(s.y, boundary), cell)), 0), grid - 1);
+  cz = min(max((int)floorf(__fdiv_rn(__fadd_rn(s.z, boundary), cell)), 0), grid - 1);
+}
+
+__device__ __forceinline__ bool spheres_overlap(float4 a, float4 b) {
+  const float fx = __fsub_rn(a.x, b.x), fy = __fsub_rn(a.y, b.y), fz = __fsub_rn(a.z, b.z);
+  const float r = __fadd_rn(a.w, b.w);
+  const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+  return d2 < __fmul_rn(r, r);
+}
+
+__global__ void k_sph_entries(const float4* __restrict__ sph, int n, float cell, float boundary, int grid,
+                              unsigned long long* __restrict__ ekey, int* __restrict__ ebody, uint32_t bmask,
+                              int* __restrict__ bcount, int* __restrict__ nentries) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *nentries = n;
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+    int cx, cy, cz;
+    sphere_cell(sph[b], cell, boundary, grid, cx, cy, cz);
+    const uint64_t k = cell_key(cx, cy, cz);
+    ekey[b] = k;
+    ebody[b] = b;
+    atomicAdd(bcount + (key_hash(k) & bmask), 1);
+  }
+}
+
+// pass 0 counts the pairs of every body, pass 1 writes them at off[i] and sorts by j
+template <int PASS>
+__global__ void k_sph_pairs(const float4* __restrict__ sph, int n, float cell, float boundary, int grid,
+                            uint32_t bmask, const int* __restrict__ boff, const int* __restrict__ bend,
+                            const unsigned long long* __restrict__ skey, const int* __restrict__ sbody,
+                            int* __restrict__ pcount, int2* __restrict__ out, int cap) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 si = sph[i];
+    int cx, cy, cz;
+    sphere_cell(si, cell, boundary, grid, cx, cy, cz);
+    int cnt = 0;
+    const int base = PASS == 1 ? pcount[i] : 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          const int x = cx + dx, y = cy + dy, z = cz + dz;
+          if (x < 0 || x >= grid || y < 0 || y >= grid || z < 0 || z >= grid) continue;
+          const uint64_t k = cell_key(x, y, z);
+          const uint32_t h = key_hash(k) & bmask;
+          for (int s = boff[h]; s < bend[h]; ++s) {
+            if (skey[s] != k) continue;
+            const int j = sbody[s];
+            if (j <= i || !spheres_overlap(si, sph[j])) continue;
+            if (PASS == 1 && base + cnt < cap) out[base + cnt] = make_int2(i, j);
+            ++cnt;
+          }
+        }
+    if (PASS == 0) {
+      pcount[i] = cnt;
+    } else {
+      const int m = min(cnt, cap - base);
+      for (int a = 1; a < m; ++a) {
+        const int2 v = out[base + a];
+        int c = a - 1;
+        while (c >= 0 && out[base + c].y > v.y) {
+          out[base + c + 1] = out[base + c];
+          --c;
+        }
+        out[base + c + 1] = v;
+      }
+    }
+  }
+}
+
 struct ogx_broad {
   ogx_ctx* ctx = nullptr;
   int max_bodies = 0;
@@ -413,6 +497,45 @@ extern "C" ogx_status ogx_broadphase(ogx_broad* B, const ogx_pool* pool, float c
   cudaSetDevice(B->ctx->device);
   return broad_run(B, B->ctx->stream, pool->d_points, pool->d_bodies, pool->nbodies, cell, margin, max_pairs,
                    d_pairs, d_result);
+}
+
+// Candidate pairs from bounding spheres with the reference's semantics (see k_sph_pairs).
+extern "C" ogx_status ogx_broadphase_spheres(ogx_broad* B, const float* d_spheres, int num_bodies, float cell,
+                                             float boundary, int grid_size, int max_pairs, gkCollisionPair* d_pairs,
+                                             int* d_result) {
+  if (!B || !d_spheres || !d_result) return ogx_fail(OGX_ERR_INVALID, "NULL broad phase, spheres or result");
+  if (num_bodies < 0 || num_bodies > B->max_bodies)
+    return ogx_fail(OGX_ERR_CAPACITY, "%d bodies for a broad phase of %d", num_bodies, B->max_bodies);
+  if (!(cell > 0.0f) || !(boundary >= 0.0f) || grid_size < 1 || grid_size >= kAxisBias || max_pairs < 0)
+    return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
+  cudaSetDevice(B->ctx->device);
+  cudaStream_t st = B->ctx->stream;
+  const int sms = B->ctx->sm_count;
+  const uint32_t bmask = B->nbuckets - 1u;
+  const float4* sph = reinterpret_cast<const float4*>(d_spheres);
+  cudaError_t e = cudaMemsetAsync(B->scal, 0, 4 * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->boff, 0, B->nbuckets * sizeof(int), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->pcount + num_bodies, 0, sizeof(int), st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "broad-phase reset");
+  const int gb = std::max(1, std::min(8 * sms, (num_bodies + 127) / 128));
+  k_sph_entries<<<gb, 128, 0, st>>>(sph, num_bodies, cell, boundary, grid_size, B->ekey, B->ebody, bmask, B->boff,
+                                    B->scal + 0);
+  e = scan(B, B->boff, (int)B->nbuckets, nullptr, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(B->bend, B->boff, B->nbuckets * sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) {
+    k_scatter<<<8 * sms, 256, 0, st>>>(B->ekey, B->ebody, B->scal + 0, bmask, B->bend, B->skey, B->sbody);
+    k_sph_pairs<0><<<gb, 128, 0, st>>>(sph, num_bodies, cell, boundary, grid_size, bmask, B->boff, B->bend, B->skey,
+                                       B->sbody, B->pcount, nullptr, 0);
+    e = scan(B, B->pcount, num_bodies + 1, B->scal + 1, st);
+  }
+  if (e == cudaSuccess)
+    k_sph_pairs<1><<<gb, 128, 0, st>>>(sph, num_bodies, cell, boundary, grid_size, bmask, B->boff, B->bend, B->skey,
+                                       B->sbody, B->pcount, reinterpret_cast<int2*>(d_pairs), max_pairs);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_result, B->scal + 1, 2 * sizeof(int), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "broad-phase launch");
+  return OGX_OK;
 }
 
 // Sub-mesh pair expansion (visualization/integrate_final_gjk.cu:265-302): body pair p of

@@ -22,8 +22,12 @@
 #if defined(__CUDACC__)
 #define OGX_HD __host__ __device__ __forceinline__
 #define OGX_D __device__ __forceinline__
+// a rarely taken path kept out of line, so that its registers do not weigh on the loop
+// that calls it
+#define OGX_COLD __host__ __device__ __noinline__
 #else
 #define OGX_HD inline
+#define OGX_COLD inline
 #endif
 
 #if !defined(__CUDACC__)

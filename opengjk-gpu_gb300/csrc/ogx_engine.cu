@@ -185,8 +185,6 @@ ogx_status init_kernels(int device) {
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = gjk_variants_d(&t);
   for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
-  n = gjk_variants_e(&t);
-  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_a(&t);
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_b(&t);
@@ -446,26 +444,13 @@ extern "C" int ogx_ctx_stage_timeline(ogx_ctx* ctx, const char** names, float* m
   return n;
 }
 
-// The counters of the last call in the layout documented in include/ogx.h (per-bucket
-// totals of the GJK and EPA lists, then the other passes' counts); the device keeps the
-// bucket counts per sub-list.
 extern "C" int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap) {
-  constexpr int kOut = 2 * kBuckets + (kCntSlots - kCntBase);
-  if (!ctx || !ctx->d_counts || cap < kOut) return 0;
-  int32_t dev[kCntSlots];
-  if (cudaMemcpyAsync(dev, ctx->d_counts, kCntSlots * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream) !=
-          cudaSuccess ||
+  if (!ctx || !ctx->d_counts || cap < kCntSlots) return 0;
+  if (cudaMemcpyAsync(counts, ctx->d_counts, kCntSlots * sizeof(int), cudaMemcpyDeviceToHost,
+                      ctx->stream) != cudaSuccess ||
       cudaStreamSynchronize(ctx->stream) != cudaSuccess)
     return -1;
-  for (int b = 0; b < kBuckets; ++b) {
-    counts[b] = counts[kBuckets + b] = 0;
-    for (int s = 0; s < kSub; ++s) {
-      counts[b] += dev[kCntGjk + b * kSub + s];
-      counts[kBuckets + b] += dev[kCntEpa + b * kSub + s];
-    }
-  }
-  for (int k = kCntBase; k < kCntSlots; ++k) counts[2 * kBuckets + k - kCntBase] = dev[k];
-  return kOut;
+  return kCntSlots;
 }
 
 ogx_status ogx_ctx::ensure_scratch(int npairs) {
@@ -474,8 +459,8 @@ ogx_status ogx_ctx::ensure_scratch(int npairs) {
   free_scratch();
   size_t cap = std::max<size_t>(1024, (size_t)npairs + npairs / 4);
   cudaError_t e;
-  if ((e = cudaMalloc(&d_lists, kBuckets * kSub * cap * sizeof(int))) != cudaSuccess ||
-      (e = cudaMalloc(&d_elists, kBuckets * kSub * cap * sizeof(int))) != cudaSuccess ||
+  if ((e = cudaMalloc(&d_lists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&d_elists, kBuckets * cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&d_polish, cap * sizeof(PolishRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine, cap * sizeof(RefineRec))) != cudaSuccess ||
       (e = cudaMalloc(&d_refine_full, cap * sizeof(int))) != cudaSuccess ||
@@ -685,7 +670,6 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.status = d_status;
   B.lists = ctx->d_lists;
   B.elists = ctx->d_elists;
-  B.nsub = kSub;
   B.counts = ctx->d_counts;
   B.polish = ctx->d_polish;
   B.refine = ctx->d_refine;

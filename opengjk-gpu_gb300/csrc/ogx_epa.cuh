@@ -176,6 +176,28 @@ OGX_HD double4 face_plane64(const Mem& M, const Bodies& B, int f) {
   return make_double4_(m.x * inv, m.y * inv, m.z * inv, dot(m, q0) * inv);
 }
 
+// Thin-contact check at FP32 convergence: true when exact supports along face f's FP64
+// plane improve on the face by more than tol.
+template <class Team, class Bodies, class Mem>
+OGX_HD bool thin_gain_exceeds(const Team& t, const Bodies& B, const Mem& M, int f, float tol) {
+  const double4 p = face_plane64(M, B, f);
+  if (!(p.w < (double)INFINITY)) return false;
+  const dv3 n64 = v3<double>(p.x, p.y, p.z);
+  double ha, hb;
+  exact_support(t, B, 0, n64, ha);
+  exact_support(t, B, 1, -n64, hb);
+  return ha + hb - p.w > (double)tol;
+}
+
+// Are faces f and g coplanar on their FP64 planes from the exact points?
+template <class Mem, class Bodies>
+OGX_HD bool faces_coplanar64(const Mem& M, const Bodies& B, int f, int g) {
+  const double4 pf = face_plane64(M, B, f), pg = face_plane64(M, B, g);
+  const double dn = ::fabs(pf.x - pg.x) + ::fabs(pf.y - pg.y) + ::fabs(pf.z - pg.z);
+  const double sc = ::fmax(1.0, ::fabs(pf.w));
+  return dn <= 1e-9 && ::fabs(pg.w - pf.w) <= 1e-12 * sc;
+}
+
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
 template <class Mem, class Bodies>
 OGX_HD float4 face_plane(const Mem& M, const Bodies& B, int a, int b, int c, bool escalate, bool all64,
@@ -300,14 +322,7 @@ OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o,
     // the exact points; a neighbour that is not -- FP32 planes made the polytope a little
     // non-convex or ranked the faces wrongly, on dense flat patches -- would give a normal
     // a few 1e-5 off and witnesses off the normal: the contact runs again on FP64 planes.
-    const double4 pf = face_plane64(M, B, f), pg = face_plane64(M, B, g2);
-    const double dn = ::fabs(pf.x - pg.x) + ::fabs(pf.y - pg.y) + ::fabs(pf.z - pg.z);
-    const double sc = ::fmax(1.0, ::fabs(pf.w));
-    if (dn <= 1e-9 && ::fabs(pg.w - pf.w) <= 1e-12 * sc) {
-      f = g2;
-      continue;
-    }
-    if (rerun_ok) return true;
+    if (!faces_coplanar64(M, B, f, g2) && rerun_ok) return true;
     f = g2;
   }
   const int2 ia = M.vid[a], ib = M.vid[b], ic = M.vid[c];
@@ -613,6 +628,8 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
   const float tol_floor = cfg.epa_tol;
   int best = -1;
   bool done = false;
+  bool thin = false;
+  float thin_tol = 0.0f;
   while (it < cfg.epa_max_iter) {
     ++it;
     // closest live face
@@ -650,17 +667,10 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
       const float tol = fmaxf(tol_floor, cfg.epa_rel * scale);
       gain = dot(n, q) - bd;
       conv = gain < tol;
-      if (conv && !all64 && escalate && can_spill && !(gain > kEpaCertGain * scale) && bd < kEpaThin * scale) {
-        // a thin contact: the FP32 test may have been fooled by the face normal's rounding
-        const double4 p = face_plane64(M, B, best);
-        if (p.w < (double)INFINITY) {
-          const dv3 n64 = v3<double>(p.x, p.y, p.z);
-          double ha, hb;
-          exact_support(t, B, 0, n64, ha);
-          exact_support(t, B, 1, -n64, hb);
-          if (ha + hb - p.w > (double)tol) gain = INFINITY;  // re-run certified below
-        }
-      }
+      // a thin contact: the FP32 test may have been fooled by the face normal's rounding;
+      // checked after the loop (its FP64 scans would weigh on the loop's registers)
+      thin = conv && !all64 && escalate && can_spill && !(gain > kEpaCertGain * scale) && bd < kEpaThin * scale;
+      thin_tol = tol;
     }
     if (conv) {
       if (!cert && escalate && can_spill && !all64 && gain > kEpaCertGain * scale) {
@@ -851,6 +861,11 @@ OGX_HD void epa_pair(const Team& t, const Bodies& B, const Config& cfg, const Gj
     best = cbest;
     t.argmin(bd, best);
     o.status |= OGX_S_EPA_CAP;
+  }
+  if (thin && best >= 0 && thin_gain_exceeds(t, B, M, best, thin_tol)) {
+    o.spill = true;
+    o.spill64 = true;
+    return;
   }
   if (best >= 0) {
     const bool rerun = !cert && escalate && can_spill && !all64;

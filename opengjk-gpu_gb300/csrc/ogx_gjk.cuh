@@ -965,10 +965,7 @@ OGX_HD void refine_begin(const Bodies& B, const GjkState& g, int max_iter, Refin
 // batch and returns a distance 1.3% too large).  Returns the reduced simplex in s (slots
 // keep their .k) and its closest point in v; s.n == 4 means the origin is enclosed.
 template <class T>
-#if defined(__CUDACC__)
-__noinline__
-#endif
-OGX_HD void closest_exhaustive(Sx<T>& s, vec3<T>& v) {
+OGX_COLD void closest_exhaustive(Sx<T>& s, vec3<T>& v) {
   const int n = s.n;
   const int nw = n - 1;
   const T zero = T(0);
@@ -1090,13 +1087,15 @@ OGX_HD void refine_step(const Bodies& B, RefineStateT<T>& r, int xa, int xb) {
   r.ib[s.n] = xb;
   s.n++;
   Unc u{false};
-  const Sx<T> grown = s;
   subdistance(s, r.v, u);
   r.lam_valid = false;
   if (s.n != 4 && !(dot(r.v, r.v) < vv * T(1.0 - 1e-12))) {
     // the region decisions made no progress although the gap says progress is possible:
-    // solve the step again by exhaustive search
-    Sx<T> t = grown;
+    // solve the step again by exhaustive search on the grown simplex
+    Sx<T> t = prev;
+    t.v[t.n].p = w;
+    t.v[t.n].k = t.n;
+    t.n++;
     vec3<T> vt;
     closest_exhaustive(t, vt);
     if (t.n == 4 || dot(vt, vt) < vv * T(1.0 - 1e-12)) {

@@ -49,7 +49,7 @@ __global__ void k_bin(DevBatch B) {
   const int n32 = (B.npairs + 31) & ~31;
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n32; p += stride) {
     const bool in = p < B.npairs;
-    int b = -1, sub = 0;
+    int b = -1;
     bool bad = false;
     bool work = false;
     if (in) {
@@ -59,7 +59,6 @@ __global__ void k_bin(DevBatch B) {
         const int na = B.bodies[pr.x].n, nb = B.bodies[pr.y].n;
         bad = na < 1 || nb < 1;
         b = bucket_of(na > nb ? na : nb);
-        if (B.nsub > 1) sub = subbin_of(b, na + nb);
       }
       if (bad) {
         mark_bad(B, p);
@@ -77,14 +76,14 @@ __global__ void k_bin(DevBatch B) {
         work = true;
       }
     }
-    // warp-aggregated append per bucket and sub-list
-    const int key = work ? b * kSub + sub : -1;
+    // warp-aggregated append per bucket
+    const int key = work ? b : -1;
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     const int wl = threadIdx.x & 31;
     const int leader = __ffs(peers) - 1;
     if (key >= 0) {
       int* ctr = B.counts + (B.mode == kModeEpa ? kCntEpa : kCntGjk) + key;
-      int* list = (B.mode == kModeEpa ? B.elists : B.lists) + ((size_t)b * B.nsub + sub) * B.npairs;
+      int* list = (B.mode == kModeEpa ? B.elists : B.lists) + (size_t)key * B.npairs;
       int base = 0;
       if (wl == leader) base = atomicAdd(ctr, __popc(peers));
       base = __shfl_sync(peers, base, leader);

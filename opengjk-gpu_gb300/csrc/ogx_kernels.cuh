@@ -27,19 +27,6 @@ OGX_HD int bucket_of(int m) {
   return m <= 16 ? 0 : m <= 32 ? 1 : m <= 64 ? 2 : m <= 128 ? 3 : m <= 256 ? 4 : m <= 512 ? 5 : 6;
 }
 
-// Each bucket's work lists are kept in kSub sub-lists by the pair's total point count
-// n1 + n2 (equal ranges of the totals the bucket can hold), consumed in order: the teams
-// that share a warp take consecutive entries, so their scans run about the same length.
-constexpr int kSub = 4;
-OGX_HD int subbin_of(int bucket, int total) {
-  // the larger count is in (lo, hi]: bucket b holds (8 * 2^b, 16 * 2^b], the last bucket
-  // from 513 points up (binned as if it ended at 1024)
-  const int lo = bucket == 0 ? 0 : (8 << bucket);
-  const int hi = 16 << bucket;
-  const int s = (total - lo - 1) * kSub / (2 * hi - lo);
-  return s < 0 ? 0 : (s >= kSub ? kSub - 1 : s);
-}
-
 // FP64 refinement request of a separated pair: the support pair along the final
 // direction and whether the FP32 pass proved it exact
 struct RefineRec {
@@ -58,18 +45,16 @@ struct PolishRec {
 enum { kModeGjk = 1, kModeGjkEpa = 2, kModeEpa = 3 };
 
 // counter slots in DevBatch::counts
-constexpr int kCntGjk = 0;                        // [0, kBuckets kSub): bucket b, sub-list s at b kSub + s
-constexpr int kCntEpa = kBuckets * kSub;          // the same for the EPA lists
-constexpr int kCntBase = 2 * kBuckets * kSub;
-constexpr int kCntPolish = kCntBase;              // EPA faces to re-solve in FP64
-constexpr int kCntRefine = kCntBase + 1;          // separated pairs to refine in FP64
-constexpr int kCntRefineFull = kCntBase + 2;      // of those, the ones to continue in FP64
-constexpr int kCntSpill = kCntBase + 3;           // contacts that outgrew the small EPA capacity
-constexpr int kCntRefineBig = kCntBase + 4;       // of the FP64 continuations, bodies > 128 points
-constexpr int kCntSpillLate = kCntBase + 5;       // contacts found by the FP64 refinement
-constexpr int kCntResume = kCntBase + 6;          // capacity spills saved for the full pass to resume
-constexpr int kCntSlots = kCntBase + 7;
-static_assert(kCntSlots <= 64, "counter area of 64 ints");
+constexpr int kCntGjk = 0;                  // [0, kBuckets)
+constexpr int kCntEpa = kBuckets;           // [kBuckets, 2 kBuckets)
+constexpr int kCntPolish = 2 * kBuckets;    // EPA faces to re-solve in FP64
+constexpr int kCntRefine = 2 * kBuckets + 1;  // separated pairs to refine in FP64
+constexpr int kCntRefineFull = 2 * kBuckets + 2;  // of those, the ones to continue in FP64
+constexpr int kCntSpill = 2 * kBuckets + 3;  // contacts that outgrew the small EPA capacity
+constexpr int kCntRefineBig = 2 * kBuckets + 4;  // of the FP64 continuations, bodies > 128 points
+constexpr int kCntSpillLate = 2 * kBuckets + 5;  // contacts found by the FP64 refinement
+constexpr int kCntResume = 2 * kBuckets + 6;  // capacity spills saved for the full pass to resume
+constexpr int kCntSlots = 2 * kBuckets + 7;
 // FP64 continuations of pairs whose bodies have at most this many points run one thread
 // per pair (FP64 instructions then serve 32 pairs); larger ones one warp per pair
 constexpr int kRefineLaneMax = 128;
@@ -85,10 +70,9 @@ struct DevBatch {
   float* dist;
   float* nrm;       // may be null in GJK mode
   int32_t* status;  // may be null
-  int* lists;       // kBuckets * nsub regions of npairs entries (bucket b, sub-list s: b nsub + s)
-  int* elists;      // the same for the contacts of each bucket
+  int* lists;       // kBuckets regions of npairs entries
+  int* elists;      // kBuckets regions of npairs entries
   int* counts;      // kCntSlots
-  int nsub;         // sub-lists per bucket: kSub, or 1 (one list per bucket)
   PolishRec* polish;
   RefineRec* refine;  // npairs entries
   int* refine_full;   // npairs entries: pair ids whose FP32 support was not certain
@@ -179,20 +163,8 @@ __device__ __forceinline__ void bind_src(MemBodies& s, const float* pool, BodyRe
   s.bind(pool, a, b);
 }
 
-// Entry j of a bucket's work (GJK or EPA lists): the bucket's sub-lists in order.  cnt[s]
-// holds the sub-list lengths; returns -1 past the end.
-__device__ __forceinline__ int list_entry(const int* lists, const int* cnt, int nsub, int bucket, int npairs, int j) {
-  for (int s = 0; s < nsub; ++s) {
-    if (j < cnt[s]) return lists[((size_t)bucket * nsub + s) * npairs + j];
-    j -= cnt[s];
-  }
-  return -1;
-}
-
-// Store one finished pair's GJK result and route it (EPA list, FP64 refinement list);
-// total = n1 + n2 of the pair (its EPA sub-list).
-__device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int total, int p, const GjkState& g,
-                                          bool lead) {
+// Store one finished pair's GJK result and route it (EPA list, FP64 refinement list).
+__device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, const GjkState& g, bool lead) {
   const bool contact = gjk_contact(g);
   if (lead) {
     store_simplex(B.smp + p, g);
@@ -202,13 +174,8 @@ __device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int tot
     // pairs sent to the FP64 refinement get their normal there
   }
   const bool to_epa = lead && B.mode == kModeGjkEpa && contact;
-  const int sub = B.nsub > 1 ? subbin_of(bucket, total) : 0;
-  // one append per sub-list (the lanes of a warp may hold pairs of different sub-lists)
-  for (int s = 0; s < B.nsub; ++s) {
-    const bool mine = to_epa && sub == s;
-    const int e = warp_append(B.counts + kCntEpa + bucket * kSub + s, mine);
-    if (mine) B.elists[((size_t)bucket * B.nsub + s) * B.npairs + e] = p;
-  }
+  const int e = warp_append(B.counts + kCntEpa + bucket, to_epa);
+  if (to_epa) B.elists[(size_t)bucket * B.npairs + e] = p;
   const int q = warp_append(B.counts + kCntRefine, lead && g.polish);
   if (lead && g.polish) {
     RefineRec r;
@@ -225,13 +192,10 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
   const WarpTeam<L> t;
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
-  int cnt[kSub], total = 0;
-  for (int s = 0; s < kSub; ++s) {
-    cnt[s] = s < B.nsub ? B.counts[kCntGjk + bucket * kSub + s] : 0;
-    total += cnt[s];
-  }
-  for (int j = team; j < total; j += nteams) {
-    const int p = list_entry(B.lists, cnt, B.nsub, bucket, B.npairs, j);
+  const int cnt = B.counts[kCntGjk + bucket];
+  const int* list = B.lists + (size_t)bucket * B.npairs;
+  for (int j = team; j < cnt; j += nteams) {
+    const int p = list[j];
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
     typename SrcOf<L, K>::type src;
@@ -243,55 +207,10 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
     }
     GjkState g;
     gjk_pair(t, src, B.cfg, g, ws.x, ws.y, B.subtab);
-    gjk_store(B, bucket, ra.n + rb.n, p, g, t.lane() == 0);
+    gjk_store(B, bucket, p, g, t.lane() == 0);
   }
 }
 
-
-// The same over a queue: a team that finishes its pair stores it and takes the next
-// while the other teams of its warp keep iterating theirs, so the teams of a warp run
-// their GJK iterations together instead of every pair of the warp waiting for the
-// slowest one before the next round starts.
-template <int L, int K, int OCC = 1>
-__global__ void __launch_bounds__(128, OCC) k_gjk_q(DevBatch B, int bucket) {
-  const WarpTeam<L> t;
-  const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
-  const int nteams = (gridDim.x * blockDim.x) / L;
-  int cnt[kSub], total = 0;
-  for (int s = 0; s < kSub; ++s) {
-    cnt[s] = s < B.nsub ? B.counts[kCntGjk + bucket * kSub + s] : 0;
-    total += cnt[s];
-  }
-  typename SrcOf<L, K>::type src;
-  GjkRun r;
-  int j = team, p = -1, npts = 0;
-  bool have = false;
-  for (;;) {
-    if (!have) {
-      if (j >= total) break;
-      p = list_entry(B.lists, cnt, B.nsub, bucket, B.npairs, j);
-      const int2 pr = B.pairs[p];
-      const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
-      bind_src<L>(src, B.pool, ra, rb, t.lane());
-      int2 ws = make_int2(0, 0);
-      if (B.warm) {
-        ws = B.warm[p];
-        if (ws.x < 0 || ws.x >= ra.n || ws.y < 0 || ws.y >= rb.n) ws = make_int2(0, 0);
-      }
-      gjk_start(src, r, ws.x, ws.y);
-      npts = ra.n + rb.n;
-      have = true;
-    }
-    gjk_iterate(t, src, B.cfg, r, B.subtab);
-    if (r.done) {
-      GjkState g;
-      gjk_end(t, src, B.cfg, r, g);
-      gjk_store(B, bucket, npts, p, g, t.lane() == 0);
-      have = false;
-      j += nteams;
-    }
-  }
-}
 
 // kFull: the full-capacity pass over the spill list -- certified re-runs where the entry
 // asks for FP64 planes, and the FP64 polish of the result done here by lane 0 instead of
@@ -359,13 +278,10 @@ __global__ void __launch_bounds__(128, OCC) k_epa(DevBatch B, int bucket) {
   EpaMemSmall& M = mem[threadIdx.x / L];
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
-  int cnt[kSub], total = 0;
-  for (int s = 0; s < kSub; ++s) {
-    cnt[s] = s < B.nsub ? B.counts[kCntEpa + bucket * kSub + s] : 0;
-    total += cnt[s];
-  }
-  for (int j = team; j < total; j += nteams) {
-    const int p = list_entry(B.elists, cnt, B.nsub, bucket, B.npairs, j);
+  const int cnt = B.counts[kCntEpa + bucket];
+  const int* list = B.elists + (size_t)bucket * B.npairs;
+  for (int j = team; j < cnt; j += nteams) {
+    const int p = list[j];
     int code = 0;
     const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true, &code);
     const bool lead = t.lane() == 0;
@@ -388,8 +304,6 @@ struct KernelInfo {
           // (fewer registers per thread, more warps)
 };
 constexpr int kOccShift = 8;
-// + (1 << kQueueShift) for a GJK variant that runs its pairs as a queue (k_gjk_q)
-constexpr int kQueueShift = 12;
 OGX_HD int variant_blocks(int K) { return K & ((1 << kOccShift) - 1); }
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
@@ -401,7 +315,6 @@ int gjk_variants_a(const KernelInfo** out);
 int gjk_variants_b(const KernelInfo** out);
 int gjk_variants_c(const KernelInfo** out);
 int gjk_variants_d(const KernelInfo** out);
-int gjk_variants_e(const KernelInfo** out);
 int epa_variants_a(const KernelInfo** out);
 int epa_variants_b(const KernelInfo** out);
 int epa_variants_c(const KernelInfo** out);

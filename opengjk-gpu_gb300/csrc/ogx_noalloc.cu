@@ -171,7 +171,6 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
   B.counts = reinterpret_cast<int*>(S->scratch + kOffCounts);
   B.lists = reinterpret_cast<int*>(S->scratch + kOffLists);
   B.elists = reinterpret_cast<int*>(S->scratch + kOffElists);
-  B.nsub = 1;  // one list per bucket: the static array is sized for that
   B.refine = reinterpret_cast<RefineRec*>(S->scratch + kOffRefine);
   B.refine_full = reinterpret_cast<int*>(S->scratch + kOffRefineFull);
   B.polish = reinterpret_cast<PolishRec*>(S->scratch + kOffPolish);

@@ -131,6 +131,7 @@ SIGNATURES = {
     "ogx_epa": (_I, [_P, _P, _I, _P, _P, _P, _P, _P]),
     "ogx_broad_create": (_I, [_P, _I, _P]),
     "ogx_broadphase": (_I, [_P, _P, ctypes.c_float, ctypes.c_float, _I, _P, _P]),
+    "ogx_broadphase_spheres": (_I, [_P, _P, _I, ctypes.c_float, ctypes.c_float, _I, _I, _P, _P]),
     "ogx_broad_destroy": (_I, [_P]),
     "ogx_gjk_epa_streamed": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _I]),
     "ogx_gjk_epa_streamed_ranges": (_I, [_P, _P, _P, _I, _P, _P, _P, _P, _P, _P, _I, _I]),

@@ -441,6 +441,26 @@ class Broad:
         count, flags = (int(x) for x in self._result.cpu().tolist())
         return pairs_dev[:min(count, max_pairs)], count, flags
 
+    def run_spheres(self, spheres_dev, cell: float, boundary: float, grid_size: int, max_pairs: int = 1 << 20):
+        """The reference's bounding-sphere pairs (ogx_broadphase_spheres): spheres_dev is a
+        float32 [n, 4] CUDA tensor (x, y, z, radius).  Returns (pairs int32 [n, 2] CUDA
+        tensor sorted by (i, j), total count)."""
+        torch = _torch()
+        assert spheres_dev.is_cuda and spheres_dev.dtype == torch.float32 and spheres_dev.is_contiguous()
+        pairs_dev = torch.empty((max(max_pairs, 1), 2), dtype=torch.int32, device=spheres_dev.device)
+        cur = torch.cuda.current_stream(spheres_dev.device)
+        if cur != self.ctx.stream:
+            self.ctx.stream.wait_stream(cur)
+        check(self.ctx.lib.ogx_broadphase_spheres(self.handle, ctypes.c_void_p(spheres_dev.data_ptr()),
+                                                  int(spheres_dev.shape[0]), ctypes.c_float(cell),
+                                                  ctypes.c_float(boundary), int(grid_size), int(max_pairs),
+                                                  ctypes.c_void_p(pairs_dev.data_ptr()),
+                                                  ctypes.c_void_p(self._result.data_ptr())))
+        if cur != self.ctx.stream:
+            cur.wait_stream(self.ctx.stream)
+        count = int(self._result.cpu()[0])
+        return pairs_dev[:min(count, max_pairs)], count
+
     def close(self):
         if self.handle and self.ctx.handle:
             self.ctx.lib.ogx_broad_destroy(self.handle)
