@@ -37,16 +37,15 @@ OGX_HD void sdot4(const float4& x, const float4& y, const float4& z, fv3 d, floa
 #endif
 }
 
-// Fold a block of 4 support values (indices i0..i0+3) into the running (best, bi): the
-// block's maximum is compared once with the running best, and only a block that beats
-// it (strictly: an equal value keeps the earlier index) looks up which of its points
-// holds the maximum, the lowest first.  Same result as comparing point by point in index
-// order; NaN values never win.
+// Fold a block of 4 support values (indices i0..i0+3) into the running (best, bi), point
+// by point in index order: a strictly greater value wins, so ties keep the lower index
+// and NaN values never win.  Written as selects (no branch for lanes to diverge on).
 OGX_HD void block_best(const float* v, int i0, float& best, int& bi) {
-  const float m = fmaxf(fmaxf(v[0], v[1]), fmaxf(v[2], v[3]));
-  if (m > best) {
-    best = m;
-    bi = v[0] == m ? i0 : (v[1] == m ? i0 + 1 : (v[2] == m ? i0 + 2 : i0 + 3));
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const bool win = v[c] > best;
+    best = win ? v[c] : best;
+    bi = win ? i0 + c : bi;
   }
 }
 

@@ -95,6 +95,9 @@ constexpr double kEpaCertTol = 1e-10;
 // exact supports along its face's FP64 plane and run again certified if they improve on
 // the face by more than that tolerance.
 constexpr float kEpaThin = 1e-3f;
+// Largest squared sine of the angle between the closest face and a neighbour the
+// origin's projection moves to, for the FP32 pass to accept the neighbour's result.
+constexpr float kEpaHopSin2 = 1e-10f;
 constexpr double kEpaCertVis = 1e-12;
 
 struct EpaOut {
@@ -187,15 +190,6 @@ OGX_HD bool thin_gain_exceeds(const Team& t, const Bodies& B, const Mem& M, int 
   exact_support(t, B, 0, n64, ha);
   exact_support(t, B, 1, -n64, hb);
   return ha + hb - p.w > (double)tol;
-}
-
-// Are faces f and g coplanar on their FP64 planes from the exact points?
-template <class Mem, class Bodies>
-OGX_HD bool faces_coplanar64(const Mem& M, const Bodies& B, int f, int g) {
-  const double4 pf = face_plane64(M, B, f), pg = face_plane64(M, B, g);
-  const double dn = ::fabs(pf.x - pg.x) + ::fabs(pf.y - pg.y) + ::fabs(pf.z - pg.z);
-  const double sc = ::fmax(1.0, ::fabs(pf.w));
-  return dn <= 1e-9 && ::fabs(pg.w - pf.w) <= 1e-12 * sc;
 }
 
 // plane of face (a, b, c): FP32, FP64 from exact points for slivers
@@ -318,11 +312,13 @@ OGX_HD bool epa_emit(const Mem& M, const Bodies& B, int f, float tie, EpaOut& o,
     if (!near) break;
     // In exact arithmetic the origin projects into the closest face of the convex
     // polytope, so a neighbour it leaves through is coplanar with it (a flat patch split
-    // into triangles: the witnesses come from the neighbour).  Decided on FP64 planes of
-    // the exact points; a neighbour that is not -- FP32 planes made the polytope a little
-    // non-convex or ranked the faces wrongly, on dense flat patches -- would give a normal
-    // a few 1e-5 off and witnesses off the normal: the contact runs again on FP64 planes.
-    if (!faces_coplanar64(M, B, f, g2) && rerun_ok) return true;
+    // into triangles -- two points of one body against two of the other make an exact
+    // parallelogram: the witnesses come from the neighbour).  A neighbour more than 1e-5
+    // rad off -- FP32 planes made the polytope a little non-convex or ranked the faces
+    // wrongly, on dense flat patches -- would give a normal up to a few 1e-4 off and
+    // witnesses off the normal: the FP32 pass runs the contact again on FP64 planes.
+    const float sx = nf.y * ng.z - nf.z * ng.y, sy = nf.z * ng.x - nf.x * ng.z, sz = nf.x * ng.y - nf.y * ng.x;
+    if (sx * sx + sy * sy + sz * sz > kEpaHopSin2 && rerun_ok) return true;
     f = g2;
   }
   const int2 ia = M.vid[a], ib = M.vid[b], ic = M.vid[c];
