@@ -142,15 +142,22 @@ def test_stress_200k_error_report(engine, orc):
     """Mixed-precision stress set at its full size (200k pairs): error of every output
     against the FP64 oracle, per kind, and every parity rule for every kind -- the
     1e-4-thick near-coplanar disks included: a thin contact's FP32 convergence is checked
-    with exact supports along its face's FP64 plane, and a face hop to a neighbour that is
-    not coplanar in FP64 is refused (the report gives how far the depth along each normal
-    that differs from the oracle's is from the oracle's depth)."""
+    with exact supports along its face's FP64 plane, and a face hop to a neighbour more
+    than 1e-5 rad off is refused by the FP32 pass, which runs the contact again certified
+    (the report gives how far the depth along each normal that differs from the oracle's
+    is from the oracle's depth)."""
     import json
+    import os
     b = W.stress(seed=9, n_pairs=200_000)
     res = engine.query(b, engine.MODE_GJK_EPA)
     o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=16)
     rep = _stress_report(b, res, o)
     print("STRESS_REPORT " + json.dumps(rep))
+    out_dir = os.environ.get("OGX_PARITY_REPORT_DIR")
+    if out_dir:  # the report of this run, for the measurement summaries
+        os.makedirs(out_dir, exist_ok=True)
+        with open(os.path.join(out_dir, "parity_stress_200k.json"), "w") as f:
+            json.dump({"workload": "stress_200k", "report": rep}, f, indent=1)
     for name, r in rep.items():
         assert r["verdict_mismatch"] == 0 and r["band_abs_violations"] == 0, (name, r)
         assert r["sep_rel_violations"] == 0, (name, r)
