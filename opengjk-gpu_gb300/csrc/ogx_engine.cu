@@ -95,6 +95,7 @@ struct Launch {
 };
 
 std::vector<Launch> g_gjkv, g_epav;  // all compiled variants
+std::vector<Launch> g_gjkp, g_epap;  // the posed kernels, one per bucket
 
 constexpr int kBlock = 128;
 constexpr int kBucketCap[kBuckets] = {16, 32, 64, 128, 256, 512, 0};
@@ -153,7 +154,8 @@ int default_choice(const std::vector<Launch>& vs, int b, bool epa) {
 }
 
 ogx_status init_variant(Launch* k, bool epa, int sms) {
-  k->smem = epa ? (size_t)(kBlock / k->L) * sizeof(EpaMemSmall) : 0;
+  const size_t staging = staging_bytes(variant_stages(k->K));
+  k->smem = epa ? ((size_t)(kBlock / k->L) * sizeof(EpaMemSmall) + 15) / 16 * 16 + staging : staging;
   cudaError_t e;
   if (k->smem > 48 * 1024) {
     e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -191,6 +193,10 @@ ogx_status init_kernels(int device) {
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   n = epa_variants_c(&t);
   for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = gjk_variants_e(&t);
+  for (int i = 0; i < n; ++i) g_gjkv.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
+  n = epa_variants_d(&t);
+  for (int i = 0; i < n; ++i) g_epav.push_back(Launch{t[i].fn, t[i].L, t[i].K, 0, 0});
   for (auto& k : g_gjkv) {
     ogx_status s = init_variant(&k, false, sms);
     if (s) return s;
@@ -198,6 +204,24 @@ ogx_status init_kernels(int device) {
   for (auto& k : g_epav) {
     ogx_status s = init_variant(&k, true, sms);
     if (s) return s;
+  }
+  {
+    const KernelInfo *pg, *pe;
+    posed_variants(&pg, &pe);
+    g_gjkp.clear();
+    g_epap.clear();
+    for (int b = 0; b < kBuckets; ++b) {
+      g_gjkp.push_back(Launch{pg[b].fn, pg[b].L, pg[b].K, 0, 0});
+      g_epap.push_back(Launch{pe[b].fn, pe[b].L, pe[b].K, 0, 0});
+    }
+    for (auto& k : g_gjkp) {
+      ogx_status s = init_variant(&k, false, sms);
+      if (s) return s;
+    }
+    for (auto& k : g_epap) {
+      ogx_status s = init_variant(&k, true, sms);
+      if (s) return s;
+    }
   }
   g_grid_bin = 4 * sms;
   g_grid_pack = 8 * sms;
@@ -647,7 +671,7 @@ extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* co
 
 ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, int nbodies,
                    int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
-                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm) {
+                   float* d_nrm, int32_t* d_status, int mode, const int2* d_warm, const float* d_xf) {
   if (npairs < 0) return ogx_fail(OGX_ERR_INVALID, "npairs < 0");
   if (npairs == 0) {
     ctx->last_launches = 0;
@@ -679,8 +703,10 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   B.resume_cap = ogx_ctx::kResumeCap;
   B.warm = d_warm;
   B.subtab = g_subtab;
+  B.xf = d_xf;
   B.cfg = ctx->cfg;
   B.mode = mode;
+  if (d_xf && mode != kModeGjkEpa) return ogx_fail(OGX_ERR_INVALID, "posed bodies: GJK + EPA calls only");
   cudaStream_t st = ctx->stream;
   int launches = 0;
   ctx->ev_count = 0;
@@ -736,7 +762,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   if (e != cudaSuccess) return ogx_cuda_fail(e, "bucket fork");
   if (mode != kModeEpa) {
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
-      const Launch& k = g_gjkv[ctx->choice[0][b]];
+      const Launch& k = d_xf ? g_gjkp[b] : g_gjkv[ctx->choice[0][b]];
       ctx->mark(kGjkName[b]);
       k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
       stage(kGjkName[b], bucket_stream(b));
@@ -753,7 +779,7 @@ ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const BodyRef* d_bodies, i
   const bool refine = mode != kModeEpa && (ctx->cfg.flags & OGX_F_FP64_POLISH);
   if (mode != kModeGjk) {
     for (int b = kBuckets - 1; b >= 0 && e == cudaSuccess; --b) {
-      const Launch& k = g_epav[ctx->choice[1][b]];
+      const Launch& k = d_xf ? g_epap[b] : g_epav[ctx->choice[1][b]];
       ctx->mark(kEpaName[b]);
       k.fn<<<fit_grid(k.grid, npairs, k.L), kBlock, k.smem, bucket_stream(b)>>>(B, b);
       stage(kEpaName[b], bucket_stream(b));

@@ -509,10 +509,11 @@ OGX_HD void simplex_weights(const GjkState& g, float* lam) {
 // FP64 re-run of one sub-distance step on the exact Minkowski points (cold path: taken
 // when an FP32 decision of the step falls inside its rounding bound).  Returns the new
 // slot order in `order` and the new direction.
+template <class Mem>
 #if defined(__CUDACC__)
 __noinline__
 #endif
-OGX_HD int escalate_step(const MemBodies B, int n, const int* ia, const int* ib, fv3 vold, int* order, fv3* vout) {
+OGX_HD int escalate_step(const Mem B, int n, const int* ia, const int* ib, fv3 vold, int* order, fv3* vout) {
   Sx<double> sd;
   sd.n = n;
   for (int j = 0; j < n; ++j) {
@@ -827,16 +828,14 @@ OGX_HD void gjk_pair(const Team& t, const Bodies& B, const Config& cfg, GjkState
 // evaluated in FP64.  Ties go to the lowest index.
 template <class Team, class Bodies, class T>
 OGX_HD int exact_support(const Team& t, const Bodies& B, int w, vec3<T> d, T& val) {
-  const MemBodies& M = B.mem_view();
+  const auto& M = B.mem_view();  // points by index (posed where the bodies are)
   const fv3 fd = v3<float>(to_float(d.x), to_float(d.y), to_float(d.z));
-  const float* X = M.base[w];
-  const float* Y = X + M.n4[w];
-  const float* Z = Y + M.n4[w];
   const int n = M.n[w];
   float m = -INFINITY, amax = 0.0f;
   for (int i = t.lane(); i < n; i += Team::L) {
-    m = fmaxf(m, sdot(X[i], Y[i], Z[i], fd));
-    amax = fmaxf(amax, fmaxf(fabsf(X[i]), fmaxf(fabsf(Y[i]), fabsf(Z[i]))));
+    const fv3 p = M.point(w, i);
+    m = fmaxf(m, sdot(p, fd));
+    amax = fmaxf(amax, fmaxf(fabsf(p.x), fmaxf(fabsf(p.y), fabsf(p.z))));
   }
   m = t.fmax_(m);
   amax = t.fmax_(amax);
@@ -848,13 +847,14 @@ OGX_HD int exact_support(const Team& t, const Bodies& B, int w, vec3<T> d, T& va
   T best = sc<T>(-INFINITY);
   int bi = 0x7fffffff;
   for (int i = t.lane(); i < n; i += Team::L) {
-    if (sdot(X[i], Y[i], Z[i], fd) < lo) continue;
+    const fv3 pf = M.point(w, i);
+    if (sdot(pf, fd) < lo) continue;
     T x;
     if constexpr (Bodies::kExact64) {
       const dv3 p = B.dpoint(w, i);
       x = p.x * d.x + p.y * d.y + p.z * d.z;
     } else {
-      x = sc<T>(X[i]) * d.x + sc<T>(Y[i]) * d.y + sc<T>(Z[i]) * d.z;
+      x = sc<T>(pf.x) * d.x + sc<T>(pf.y) * d.y + sc<T>(pf.z) * d.z;
     }
     if (x > best || (x == best && i < bi)) {
       best = x;

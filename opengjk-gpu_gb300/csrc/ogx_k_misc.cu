@@ -112,9 +112,34 @@ __device__ void refine_store(const DevBatch& B, int p, const BodyRef& ra, const 
   }
 }
 
+// The pair's bodies for the FP64 passes: as stored, or posed (the posed pipeline)
+__device__ __forceinline__ void bind_mem(MemBodies& mb, const DevBatch& B, int2, BodyRef ra, BodyRef rb) {
+  mb.bind(B.pool, ra, rb);
+}
+__device__ __forceinline__ void bind_mem(Posed<MemBodies>& mb, const DevBatch& B, int2 pr, BodyRef ra,
+                                         BodyRef rb) {
+  mb.bind_posed(B.pool, ra, rb, B.xf + 12 * (size_t)pr.x, B.xf + 12 * (size_t)pr.y);
+}
+// lane j's bodies, for a scan by the whole warp
+__device__ __forceinline__ void shfl_bodies(MemBodies& to, const MemBodies& from, int j) {
+  for (int w = 0; w < 2; ++w) {
+    to.base[w] = reinterpret_cast<const float*>(
+        __shfl_sync(0xffffffffu, reinterpret_cast<long long>(from.base[w]), j));
+    to.n[w] = __shfl_sync(0xffffffffu, from.n[w], j);
+    to.n4[w] = __shfl_sync(0xffffffffu, from.n4[w], j);
+  }
+}
+__device__ __forceinline__ void shfl_bodies(Posed<MemBodies>& to, const Posed<MemBodies>& from, int j) {
+  shfl_bodies(static_cast<MemBodies&>(to), static_cast<const MemBodies&>(from), j);
+  for (int w = 0; w < 2; ++w)
+    to.xf[w] = reinterpret_cast<const float*>(
+        __shfl_sync(0xffffffffu, reinterpret_cast<long long>(from.xf[w]), j));
+}
+
 // Re-solve of separated pairs (one thread per pair).  Pairs whose final support the GJK
 // kernel proved exact only need the exact closest point of their simplex, computed in
 // double-float arithmetic; the others are passed to k_refine_lane / k_refine_full.
+template <bool kPosed>
 __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
   const int cnt = B.counts[kCntRefine];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
@@ -132,8 +157,8 @@ __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
       }
       continue;
     }
-    MemBodies mb;
-    mb.bind(B.pool, ra, rb);
+    typename PoseOf<kPosed, MemBodies>::type mb;
+    bind_mem(mb, B, pr, ra, rb);
     GjkState g;
     load_simplex(B.smp + p, B.dist[p], g);
     g.certain = true;
@@ -146,14 +171,15 @@ __global__ void __launch_bounds__(128) k_refine(DevBatch B) {
 // FP64 continuation of GJK for the pairs with an uncertain FP32 support and bodies of
 // at most kRefineLaneMax points: one thread per pair, so that each FP64 instruction
 // serves 32 pairs (FP64 issues at 1/64 of the FP32 rate here).
+template <bool kPosed>
 __global__ void __launch_bounds__(128) k_refine_lane(DevBatch B) {
   const int cnt = B.counts[kCntRefineFull];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const int p = B.refine_full[k];
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
-    MemBodies mb;
-    mb.bind(B.pool, ra, rb);
+    typename PoseOf<kPosed, MemBodies>::type mb;
+    bind_mem(mb, B, pr, ra, rb);
     GjkState g;
     load_simplex(B.smp + p, B.dist[p], g);
     g.certain = false;
@@ -167,6 +193,7 @@ __global__ void __launch_bounds__(128) k_refine_lane(DevBatch B) {
 // runs the exact-support scans of every unfinished pair with all 32 lanes (pair j's
 // bodies and direction broadcast from lane j), then each lane takes its own pair's FP64
 // sub-distance step, so the scalar FP64 work serves 32 pairs per instruction.
+template <bool kPosed>
 __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
   const WarpTeam<32> t;
   const unsigned full = 0xffffffffu;
@@ -179,8 +206,8 @@ __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
     const bool valid = k < cnt;
     int p = -1;
     BodyRef ra{0u, 1}, rb{0u, 1};
-    MemBodies mb;
-    mb.bind(B.pool, ra, rb);
+    typename PoseOf<kPosed, MemBodies>::type mb;
+    bind_mem(mb, B, make_int2(0, 0), ra, rb);  // never scanned: this lane's r.done stays set
     GjkState g;
     RefineState r;
     r.done = true;
@@ -189,7 +216,7 @@ __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
       const int2 pr = B.pairs[p];
       ra = B.bodies[pr.x];
       rb = B.bodies[pr.y];
-      mb.bind(B.pool, ra, rb);
+      bind_mem(mb, B, pr, ra, rb);
       load_simplex(B.smp + p, B.dist[p], g);
       g.certain = false;
       refine_begin(mb, g, kRefineIters, r);
@@ -200,13 +227,8 @@ __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
       int my_xa = 0, my_xb = 0;
       for (unsigned mm = m; mm != 0u; mm &= mm - 1u) {
         const int j = __ffs(mm) - 1;
-        MemBodies bj;
-        for (int w = 0; w < 2; ++w) {
-          bj.base[w] = reinterpret_cast<const float*>(
-              __shfl_sync(full, reinterpret_cast<long long>(mb.base[w]), j));
-          bj.n[w] = __shfl_sync(full, mb.n[w], j);
-          bj.n4[w] = __shfl_sync(full, mb.n4[w], j);
-        }
+        typename PoseOf<kPosed, MemBodies>::type bj;
+        shfl_bodies(bj, mb, j);
         const dv3 vj = v3<double>(__shfl_sync(full, r.v.x, j), __shfl_sync(full, r.v.y, j),
                                   __shfl_sync(full, r.v.z, j));
         double va, vb;
@@ -226,14 +248,15 @@ __global__ void __launch_bounds__(128) k_refine_full(DevBatch B) {
   }
 }
 
+template <bool kPosed>
 __global__ void __launch_bounds__(128) k_polish(DevBatch B) {
   const int cnt = B.counts[kCntPolish];
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += gridDim.x * blockDim.x) {
     const PolishRec r = B.polish[k];
     const int p = r.pair;
     const int2 pr = B.pairs[p];
-    MemBodies mb;
-    mb.bind(B.pool, B.bodies[pr.x], B.bodies[pr.y]);
+    typename PoseOf<kPosed, MemBodies>::type mb;
+    bind_mem(mb, B, pr, B.bodies[pr.x], B.bodies[pr.y]);
     gkSimplex* s = B.smp + p;
     {
       EpaOut o;
@@ -277,6 +300,7 @@ cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st) {
 // expansion met an inconsistent horizon or stopped short of the FP32 rounding level; or
 // (late != 0) over the contacts the FP64 refinement found, all certified.  One warp per
 // contact, points read from memory (any body size).
+template <bool kPosed>
 __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B, int late) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMemCert* mem = reinterpret_cast<EpaMemCert*>(smem_raw);
@@ -291,26 +315,33 @@ __global__ void __launch_bounds__(128) k_epa_spill(DevBatch B, int late) {
     const int e = late ? B.spill[B.npairs - 1 - j] : B.spill[j];
     if (e & kSpillResume) {  // continue the small pass's saved expansion
       const EpaResume* rs = B.resume + (e & (kSpillResume - 1));
-      epa_item<32, 0, true>(t, B, B.cfg, rs->pair, M, false, nullptr, rs);
+      epa_item<32, 0, true, 0, kPosed>(t, B, B.cfg, rs->pair, M, false, nullptr, rs);
     } else {
-      epa_item<32, 0, true>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
+      epa_item<32, 0, true, 0, kPosed>(t, B, (e & kSpill64) ? cfg64 : B.cfg, e & ~kSpill64, M, false);
     }
     t.sync();
   }
 }
 
+// the launchers run the posed kernels when the batch carries poses (B.xf)
 cudaError_t launch_epa_spill(const DevBatch& B, int grid, cudaStream_t st, bool late) {
-  k_epa_spill<<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B, late ? 1 : 0);
+  if (B.xf)
+    k_epa_spill<true><<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B, late ? 1 : 0);
+  else
+    k_epa_spill<false><<<grid, 128, 4 * sizeof(EpaMemCert), st>>>(B, late ? 1 : 0);
   return cudaGetLastError();
 }
 
 cudaError_t epa_spill_occupancy(int block, int* per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_epa_spill, block,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_epa_spill<false>, block,
                                                        (block / 32) * sizeof(EpaMemCert));
 }
 
 cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
-  k_polish<<<grid, 128, 0, st>>>(B);
+  if (B.xf)
+    k_polish<true><<<grid, 128, 0, st>>>(B);
+  else
+    k_polish<false><<<grid, 128, 0, st>>>(B);
   return cudaGetLastError();
 }
 
@@ -318,24 +349,32 @@ cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st) {
 // run on st and st2 (the same stream when st2 == st; the caller joins st2 back)
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st, cudaStream_t st2,
                           cudaEvent_t routed) {
-  k_refine<<<grid, 128, 0, st>>>(B);
+  if (B.xf)
+    k_refine<true><<<grid, 128, 0, st>>>(B);
+  else
+    k_refine<false><<<grid, 128, 0, st>>>(B);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && st2 != st) {
     e = cudaEventRecord(routed, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, routed, 0);
   }
   if (e != cudaSuccess) return e;
-  k_refine_lane<<<grid, 128, 0, st>>>(B);
-  k_refine_full<<<grid_full, 128, 0, st2>>>(B);
+  if (B.xf) {
+    k_refine_lane<true><<<grid, 128, 0, st>>>(B);
+    k_refine_full<true><<<grid_full, 128, 0, st2>>>(B);
+  } else {
+    k_refine_lane<false><<<grid, 128, 0, st>>>(B);
+    k_refine_full<false><<<grid_full, 128, 0, st2>>>(B);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t refine_occupancy(int block, int* per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_refine, block, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_refine<false>, block, 0);
 }
 
 cudaError_t polish_occupancy(int block, int* per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_polish, block, 0);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_polish<false>, block, 0);
 }
 
 }  // namespace ogx

@@ -82,6 +82,8 @@ struct DevBatch {
   int resume_cap;
   const int2* warm;   // optional: GJK start vertex indices per pair (out of range: ignored)
   const uint32_t* subtab;  // sub-distance decision table (fill_subtab); null: the tree
+  const float* xf;    // posed kernels only: 12 floats per body (R row-major, t), the pool
+                      // then holds the bodies in their own frame
   ogx_config cfg;
   int mode;
 };
@@ -142,25 +144,69 @@ __device__ __forceinline__ void store3(float* p, fv3 v) {
 }
 
 // ---------------------------------------------------------------------------------
-// source of body points for bucket kernels: registers (K > 0) or memory (K == 0)
-template <int L, int K>
+// source of body points for bucket kernels: registers (K > 0), memory (K == 0), or
+// memory staged through D shared-memory slots per lane (K == 0, D > 0)
+template <int L, int K, int D = 0>
 struct SrcOf {
   typedef RegBodies<L, K> type;
 };
 template <int L>
-struct SrcOf<L, 0> {
+struct SrcOf<L, 0, 0> {
   typedef MemBodies type;
 };
+template <int L, int D>
+struct SrcOf<L, 0, D> {
+  typedef StagedBodies<L, D> type;
+};
 
+// the GJK kernels' memory scans keep four blocks per lane in flight
+template <int L, int K, int D = 0>
+struct GjkSrcOf {
+  typedef typename SrcOf<L, K, D>::type type;
+};
+template <int L>
+struct GjkSrcOf<L, 0, 0> {
+  typedef WideMemBodies type;
+};
+// posed kernel variants (memory scans only): the source of the plain variant with the
+// poses applied on the fly
+template <bool kPosed, class Src>
+struct PoseOf {
+  typedef Src type;
+};
+template <class Src>
+struct PoseOf<true, Src> {
+  typedef Posed<Src> type;
+};
+
+// shared memory of the staging slots of a block of kStageStride threads
+OGX_HD constexpr size_t staging_bytes(int D) { return D > 0 ? (size_t)(D + 1) * 3 * sizeof(float4) * kStageStride : 0; }
+
+// xa, xb: the poses of the pair's bodies (read by posed sources only)
 template <int L, int K>
 __device__ __forceinline__ void bind_src(RegBodies<L, K>& s, const float* pool, BodyRef a,
-                                         BodyRef b, int lane) {
+                                         BodyRef b, int lane, float4*, const float*, const float*) {
   s.bind(pool, a, b, lane);
 }
 template <int L>
 __device__ __forceinline__ void bind_src(MemBodies& s, const float* pool, BodyRef a, BodyRef b,
-                                         int) {
+                                         int, float4*, const float*, const float*) {
   s.bind(pool, a, b);
+}
+template <int L, int D>
+__device__ __forceinline__ void bind_src(StagedBodies<L, D>& s, const float* pool, BodyRef a,
+                                         BodyRef b, int lane, float4* slots, const float*, const float*) {
+  s.bind(pool, a, b, lane, slots);
+}
+template <int L, class Base>
+__device__ __forceinline__ void bind_src(Posed<Base>& s, const float* pool, BodyRef a, BodyRef b,
+                                         int, float4*, const float* xa, const float* xb) {
+  s.bind_posed(pool, a, b, xa, xb);
+}
+// the pose of body i (posed kernels), or null
+template <bool kPosed>
+__device__ __forceinline__ const float* pose_of(const DevBatch& B, int i) {
+  return kPosed ? B.xf + 12 * (size_t)i : nullptr;
 }
 
 // Store one finished pair's GJK result and route it (EPA list, FP64 refinement list).
@@ -187,8 +233,10 @@ __device__ __forceinline__ void gjk_store(const DevBatch& B, int bucket, int p, 
   }
 }
 
-template <int L, int K, int OCC = 1>
-__global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
+template <int L, int K, int OCC = 1, int D = 0, bool kPosed = false>
+__global__ void __launch_bounds__(kStageStride, OCC) k_gjk(DevBatch B, int bucket) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];  // staging slots (D > 0)
+  float4* slots = reinterpret_cast<float4*>(smem_raw) + threadIdx.x;
   const WarpTeam<L> t;
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
@@ -198,8 +246,8 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
     const int p = list[j];
     const int2 pr = B.pairs[p];
     const BodyRef ra = B.bodies[pr.x], rb = B.bodies[pr.y];
-    typename SrcOf<L, K>::type src;
-    bind_src<L>(src, B.pool, ra, rb, t.lane());
+    typename PoseOf<kPosed, typename GjkSrcOf<L, K, D>::type>::type src;
+    bind_src<L>(src, B.pool, ra, rb, t.lane(), slots, pose_of<kPosed>(B, pr.x), pose_of<kPosed>(B, pr.y));
     int2 ws = make_int2(0, 0);
     if (B.warm) {
       ws = B.warm[p];
@@ -209,6 +257,7 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
     gjk_pair(t, src, B.cfg, g, ws.x, ws.y, B.subtab);
     gjk_store(B, bucket, p, g, t.lane() == 0);
   }
+  if constexpr (D > 0) cp_async_wait<0>();  // no copy outlives the block
 }
 
 
@@ -219,13 +268,14 @@ __global__ void __launch_bounds__(128, OCC) k_gjk(DevBatch B, int bucket) {
 constexpr int kSpill64 = 1 << 30;      // the re-run solves every face plane in FP64
 constexpr int kSpillResume = 1 << 29;  // low bits: the EpaResume record to continue
 
-template <int L, int K, bool kFull = false, class Mem>
+template <int L, int K, bool kFull = false, int D = 0, bool kPosed = false, class Mem>
 __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B, const Config& cfg, int p,
                                          Mem& M, bool can_spill, int* spill_code = nullptr,
-                                         const EpaResume* rs = nullptr) {
+                                         const EpaResume* rs = nullptr, float4* slots = nullptr) {
   const int2 pr = B.pairs[p];
-  typename SrcOf<L, K>::type src;
-  bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane());
+  typename PoseOf<kPosed, typename SrcOf<L, K, D>::type>::type src;
+  bind_src<L>(src, B.pool, B.bodies[pr.x], B.bodies[pr.y], t.lane(), slots, pose_of<kPosed>(B, pr.x),
+              pose_of<kPosed>(B, pr.y));
   GjkState g;
   load_simplex(B.smp + p, B.dist[p], g);
   EpaOut o;
@@ -270,10 +320,15 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
 // EPA over one bucket's contacts with the small working set (EpaMemSmall per team in
 // shared memory); contacts that need more than kEpaSmallIters expansions, or whose FP32
 // expansion met an inconsistent horizon, go to the spill list
-template <int L, int K, int OCC = 1>
-__global__ void __launch_bounds__(128, OCC) k_epa(DevBatch B, int bucket) {
+// shared memory of k_epa: the teams' working sets, then the staging slots (D > 0)
+template <int L>
+OGX_HD constexpr size_t epa_mem_bytes() { return ((kStageStride / L) * sizeof(EpaMemSmall) + 15) / 16 * 16; }
+
+template <int L, int K, int OCC = 1, int D = 0, bool kPosed = false>
+__global__ void __launch_bounds__(kStageStride, OCC) k_epa(DevBatch B, int bucket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   EpaMemSmall* mem = reinterpret_cast<EpaMemSmall*>(smem_raw);
+  float4* slots = reinterpret_cast<float4*>(smem_raw + epa_mem_bytes<L>()) + threadIdx.x;
   const WarpTeam<L> t;
   EpaMemSmall& M = mem[threadIdx.x / L];
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
@@ -283,12 +338,13 @@ __global__ void __launch_bounds__(128, OCC) k_epa(DevBatch B, int bucket) {
   for (int j = team; j < cnt; j += nteams) {
     const int p = list[j];
     int code = 0;
-    const bool ok = epa_item<L, K>(t, B, B.cfg, p, M, true, &code);
+    const bool ok = epa_item<L, K, false, D, kPosed>(t, B, B.cfg, p, M, true, &code, nullptr, slots);
     const bool lead = t.lane() == 0;
     const int q = warp_append(B.counts + kCntSpill, lead && !ok);
     if (lead && !ok) B.spill[q] = code;
     t.sync();  // the next pair reuses M
   }
+  if constexpr (D > 0) cp_async_wait<0>();  // no copy outlives the block
 }
 
 // ---------------------------------------------------------------------------------
@@ -302,9 +358,13 @@ struct KernelInfo {
   int K;  // float4 blocks per lane and body kept in registers (0: read from memory);
           // + 256 * m for a variant compiled for at least m resident blocks per SM
           // (fewer registers per thread, more warps)
+          // + 65536 * D for a memory variant that stages D blocks per lane through
+          // shared memory
 };
 constexpr int kOccShift = 8;
+constexpr int kStageShift = 16;
 OGX_HD int variant_blocks(int K) { return K & ((1 << kOccShift) - 1); }
+OGX_HD int variant_stages(int K) { return K >> kStageShift; }
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
 // (L, K) can serve a bucket whose bodies have at most 4 L K points (K = 0: any size, the
@@ -315,9 +375,13 @@ int gjk_variants_a(const KernelInfo** out);
 int gjk_variants_b(const KernelInfo** out);
 int gjk_variants_c(const KernelInfo** out);
 int gjk_variants_d(const KernelInfo** out);
+int gjk_variants_e(const KernelInfo** out);
 int epa_variants_a(const KernelInfo** out);
 int epa_variants_b(const KernelInfo** out);
 int epa_variants_c(const KernelInfo** out);
+int epa_variants_d(const KernelInfo** out);
+// the posed kernels (ogx_k_posed.cu): one GJK and one EPA variant per bucket
+void posed_variants(const KernelInfo** gjk, const KernelInfo** epa);
 
 // non-template kernels (ogx_k_misc.cu)
 cudaError_t launch_refine(const DevBatch& B, int grid, int grid_full, cudaStream_t st, cudaStream_t st2,

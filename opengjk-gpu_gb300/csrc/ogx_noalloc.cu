@@ -179,6 +179,7 @@ extern "C" ogx_status ogx_gjk_epa_noalloc(const float* d_points, const void* d_b
   B.resume_cap = 0;
   B.warm = nullptr;
   B.subtab = nullptr;  // the decision tree (same outcomes as the engine's table)
+  B.xf = nullptr;
   B.cfg = c;
   B.mode = kModeGjkEpa;
 
