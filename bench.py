@@ -492,8 +492,36 @@ def serving_report(device: int, seed: int = 77, slots: int = 4, max_in_flight: i
             lat_b[-1].release()
             lat_b[-1].lag_ms = lagb[k]
         thr.join()
+
+        # world copy against the transform fused into the kernels (the same 200k-pair
+        # ticks): one tick at a time, from the pose upload to results in host memory
+        def alone(server, reps=30):
+            out = []
+            for k in range(reps):
+                i = big[k % len(big)]
+                t1 = time.perf_counter()
+                r = server.wait(server.submit(server.set_transforms(xfs[i]), lists[i]))
+                out.append((time.perf_counter() - t1) * 1e3)
+                r.release()
+            return out
+        alone(srv, 6)
+        alone_copy = alone(srv)
     finally:
         srv.close()
+    fsrv = serving.Server(scene.counts, scene.local, device=device, slots=slots, slot_pairs=262144,
+                          max_pairs_in_flight=max_in_flight, world_slots=8, warm_start=True, fused_transform=True)
+    try:
+        srv = fsrv
+        burst(range(n_lists))
+        dt_fbig = burst(big)
+        alone(fsrv, 6)
+        alone_fused = alone(fsrv)
+        lat_fbig, thr_fbig = run(big, big_rate, 100, seed + 2)
+    finally:
+        fsrv.close()
+
+    def pct(v):
+        return {"p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99))}
     return {
         "bodies": scene.n_bodies, "mean_vertices": float(scene.counts.mean()),
         "tick_pairs": "log-uniform [1k, 200k] (phase 1), 200k (phase 2)",
@@ -505,6 +533,14 @@ def serving_report(device: int, seed: int = 77, slots: int = 4, max_in_flight: i
         "broadphase_ticks": {"rate_hz": broad_rate, "ticks": len(lat_b), "cell": cell, "margin": margin,
                              "mean_pairs_per_tick": float(np.mean(found)),
                              "capacity_ticks_per_s": cap_broad_hz, **latency_summary(lat_b)},
+        "transform_fused_vs_world_copy": {
+            "what": "200k-pair ticks: world copy per pose version (k_transform) against the pose applied "
+                    "by the GJK/EPA kernels as they read the points (fused_transform); alone = one tick at "
+                    "a time, pose upload to results in host memory; poisson = the ticks_200k load",
+            "world_copy": {"alone": pct(alone_copy), "capacity_200k_ticks_per_s": cap_big_hz},
+            "fused": {"alone": pct(alone_fused), "capacity_200k_ticks_per_s": len(big) / dt_fbig,
+                      "poisson": {"rate_hz": big_rate, "pairs_per_s": thr_fbig, **latency_summary(lat_fbig)}},
+        },
         "latency": "submit -> results in host memory, host clock; phases: queued for a slot, host "
                    "staging, device (events around the request's work), rest (issue and completion "
                    "detection)",

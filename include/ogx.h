@@ -345,6 +345,11 @@ typedef struct ogx_server_config {
   int world_slots;         /* world-space copies of the pool (transform versions kept) */
   int warm_start;          /* 1: warm-start GJK from the previous simplex of the pair */
   int warm_capacity_log2;  /* warm-start table entries (16 B each) */
+  int fused_transform;     /* 1: no world copies; the GJK/EPA kernels apply each body's
+                            * pose as they read its points (world point R p + t in FP32,
+                            * one fused multiply-add chain per coordinate; support scans
+                            * rotate the direction into the body frame instead).  Pair
+                            * requests only: broad-phase requests need the world copy. */
 } ogx_server_config;
 
 void ogx_server_config_default(ogx_server_config* sc);

@@ -7,7 +7,8 @@
 //  * the bodies live on the device in their own frame (the local pool); a transform
 //    update writes a world-space copy of the pool into one of `world_slots` ring
 //    buffers with one kernel (version = tick number), so requests of older ticks still
-//    in flight keep reading their own copy;
+//    in flight keep reading their own copy; with `fused_transform` it uploads the poses
+//    only and the GJK/EPA kernels apply them as they read the points (posed kernels);
 //  * requests (a pair list of one tick) are queued; a scheduler thread admits the oldest
 //    queued request as soon as a slot (stream + device buffers for `slot_pairs` pairs) is
 //    free and the pairs in flight stay within `max_pairs_in_flight`; admitted requests
@@ -302,8 +303,11 @@ bool ogx_server::launch_narrow(Request* r, Slot& s, int w) {
     r->err = ogx_cuda_fail(e, "server request launch");
     return false;
   }
-  ogx_status os = n > 0 ? ogx_run(s.ctx, d_world[w], local->d_bodies, local->nbodies, n, s.d_pairs, s.d_smp, s.d_dist,
-                                  s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr)
+  // fused transform: the bodies as stored, with the version's poses
+  const float* pts = sc.fused_transform ? local->d_points : d_world[w];
+  const float* xf = sc.fused_transform ? d_xf[w] : nullptr;
+  ogx_status os = n > 0 ? ogx_run(s.ctx, pts, local->d_bodies, local->nbodies, n, s.d_pairs, s.d_smp, s.d_dist,
+                                  s.d_nrm, s.d_status, kModeGjkEpa, sc.warm_start ? s.d_warm : nullptr, xf)
                         : OGX_OK;
   if (os) {
     r->err = os;
@@ -498,6 +502,7 @@ extern "C" void ogx_server_config_default(ogx_server_config* sc) {
   sc->world_slots = 4;
   sc->warm_start = 1;
   sc->warm_capacity_log2 = 22;
+  sc->fused_transform = 0;
 }
 
 extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const ogx_server_config* scfg,
@@ -509,7 +514,8 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
   ogx_server_config_default(&sc);
   if (scfg) sc = *scfg;
   if (sc.slots < 1 || sc.slots > 64 || sc.slot_pairs < 1 || sc.world_slots < 2 || sc.world_slots > 64 ||
-      sc.max_pairs_in_flight < sc.slot_pairs || sc.warm_capacity_log2 < 10 || sc.warm_capacity_log2 > 30)
+      sc.max_pairs_in_flight < sc.slot_pairs || sc.warm_capacity_log2 < 10 || sc.warm_capacity_log2 > 30 ||
+      sc.fused_transform < 0 || sc.fused_transform > 1)
     return ogx_fail(OGX_ERR_INVALID, "server config out of range");
   ogx_server* S = new ogx_server();
   S->sc = sc;
@@ -668,7 +674,7 @@ extern "C" ogx_status ogx_server_set_transforms(ogx_server* S, const float* xf, 
     std::memcpy(S->h_xf[w], xf, bytes);
     e = cudaMemcpyAsync(S->d_xf[w], S->h_xf[w], bytes, cudaMemcpyHostToDevice, S->pctx->stream);
   }
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && !S->sc.fused_transform) {
     k_transform<<<8 * S->pctx->sm_count, 256, 0, S->pctx->stream>>>(S->local->d_points, S->local->d_bodies,
                                                                      S->local->nbodies, S->d_xf[w], S->d_world[w]);
     e = cudaGetLastError();
@@ -762,6 +768,8 @@ extern "C" ogx_status ogx_server_submit_broadphase(ogx_server* S, int64_t versio
   if (!S || !ticket) return ogx_fail(OGX_ERR_INVALID, "NULL argument");
   if (!(cell > 0.0f) || !(margin >= 0.0f) || max_pairs < 1)
     return ogx_fail(OGX_ERR_INVALID, "bad broad-phase arguments");
+  if (S->sc.fused_transform)
+    return ogx_fail(OGX_ERR_INVALID, "broad-phase requests read the world copy, which a fused-transform server does not keep");
   Request* r = new Request();
   r->broad = true;
   r->cell = cell;
@@ -806,6 +814,8 @@ extern "C" ogx_status ogx_server_world_layout(ogx_server* S, int64_t version, fl
   const int w = (int)(version % S->sc.world_slots);
   if (version < 0 || S->world_version[w] != version)
     return ogx_fail(OGX_ERR_INVALID, "transform version %lld is not resident", (long long)version);
+  if (S->sc.fused_transform)
+    return ogx_fail(OGX_ERR_INVALID, "a fused-transform server keeps no world copy");
   *d_points = S->d_world[w];
   *d_bodies = S->local->d_bodies;
   return OGX_OK;

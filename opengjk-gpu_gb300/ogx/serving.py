@@ -18,7 +18,8 @@ P = ctypes.c_void_p
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_int), ("slot_pairs", ctypes.c_int), ("max_pairs_in_flight", ctypes.c_int),
-                ("world_slots", ctypes.c_int), ("warm_start", ctypes.c_int), ("warm_capacity_log2", ctypes.c_int)]
+                ("world_slots", ctypes.c_int), ("warm_start", ctypes.c_int), ("warm_capacity_log2", ctypes.c_int),
+                ("fused_transform", ctypes.c_int)]
 
 
 def _bind(lib):
@@ -135,15 +136,18 @@ class Request:
 class Server:
     def __init__(self, counts, local_xyz, config: _lib.Config | None = None, device: int = 0, slots: int = 4,
                  slot_pairs: int = 262144, max_pairs_in_flight: int = 1 << 20, world_slots: int = 4,
-                 warm_start: bool = True, warm_capacity_log2: int = 22, result_sets: int | None = None):
+                 warm_start: bool = True, warm_capacity_log2: int = 22, result_sets: int | None = None,
+                 fused_transform: bool = False):
         """`result_sets` page-locked result sets of `slot_pairs` pairs are allocated up
-        front (default 2 x slots) and recycled by Request.release()."""
+        front (default 2 x slots) and recycled by Request.release().  `fused_transform`:
+        keep no world copies, the kernels apply the poses as they read the points."""
         self.lib = _lib.load()
         _bind(self.lib)
         sc = ServerConfig()
         self.lib.ogx_server_config_default(ctypes.byref(sc))
         sc.slots, sc.slot_pairs, sc.max_pairs_in_flight = slots, slot_pairs, max_pairs_in_flight
         sc.world_slots, sc.warm_start, sc.warm_capacity_log2 = world_slots, int(warm_start), warm_capacity_log2
+        sc.fused_transform = int(fused_transform)
         self.counts = np.ascontiguousarray(counts, np.int32)
         local = np.ascontiguousarray(local_xyz, np.float32)
         h = P()
@@ -170,9 +174,10 @@ class Server:
         t = ctypes.c_int64()
         bufs, pooled = self._sets.take(n)
         req = Request(0, pairs, n, bufs, self._sets if pooled else None)
-        _lib.check(self.lib.ogx_server_submit(self.handle, int(version), n, pairs.ctypes.data,
-                                              req.simplex.ctypes.data, req.dist.ctypes.data,
-                                              req.normal.ctypes.data, req.status.ctypes.data, ctypes.byref(t)))
+        self._refused(req, self.lib.ogx_server_submit(self.handle, int(version), n, pairs.ctypes.data,
+                                                      req.simplex.ctypes.data, req.dist.ctypes.data,
+                                                      req.normal.ctypes.data, req.status.ctypes.data,
+                                                      ctypes.byref(t)))
         req.ticket = t.value
         self._live[req.ticket] = req  # the arrays must outlive the request
         return req
@@ -186,13 +191,21 @@ class Server:
         req = Request(0, None, max_pairs, bufs, self._sets if pooled else None)
         req.pairs = bufs["pairs"][1][:max_pairs]
         req.count = bufs["count"][1]
-        _lib.check(self.lib.ogx_server_submit_broadphase(
+        self._refused(req, self.lib.ogx_server_submit_broadphase(
             self.handle, int(version), float(cell), float(margin), int(max_pairs), req.pairs.ctypes.data,
             req.count.ctypes.data, req.simplex.ctypes.data, req.dist.ctypes.data, req.normal.ctypes.data,
             req.status.ctypes.data, ctypes.byref(t)))
         req.ticket = t.value
         self._live[req.ticket] = req
         return req
+
+    @staticmethod
+    def _refused(req: Request, rc: int):
+        """A submit the server refused: its result set goes back to the pool, then raise."""
+        if rc != 0:
+            req.done = True
+            req.release()
+        _lib.check(rc)
 
     def done(self, req: Request) -> bool:
         d = ctypes.c_int()

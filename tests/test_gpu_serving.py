@@ -292,3 +292,62 @@ def test_non_finite_pose_refused(scene):
             srv.set_transforms(xf)
         req = srv.wait(srv.submit(v, scene.candidate_pairs(1, 500)))
         assert np.isfinite(req.dist).all()
+
+
+def test_fused_transform_matches_host_build(scene, twin):
+    """A fused-transform server (no world copy: the kernels apply each body's pose as
+    they read its points) gives the host build's posed pipeline results on the same
+    request, as the world-frame kernels give the host build's world-frame results."""
+    xf = scene.transforms(7)
+    pairs = scene.candidate_pairs(7, 12000)
+    with _server(scene, warm_start=False, fused_transform=True) as srv:
+        req = srv.wait(srv.submit(srv.set_transforms(xf), pairs))
+        res = _copy(req)
+    h = twin.run(W.Batch(scene.local, scene.offsets, scene.counts, pairs, "serving"), xf=xf)
+    same = res["dist"] == h["dist"]
+    assert same.mean() > 0.995, same.mean()
+    close = np.abs(res["dist"].astype(np.float64) - h["dist"]) <= 1e-6 * np.maximum(1, np.abs(h["dist"]))
+    assert close.mean() > 0.999
+
+
+def test_fused_transform_parity(scene, orc, twin):
+    """Fused-transform ticks with warm starts meet every parity rule against the FP64
+    oracle on their world points (pose_point of every body point), and agree with a
+    world-copy server's results on the same tick.  The two servers' world points differ
+    in their last bits (an FP32 multiply-add chain against a product rounded once from
+    FP64: about one ulp of coordinates up to 50), so the comparison allows twice that
+    difference on top of the parity tolerances."""
+    with _server(scene, warm_start=True, fused_transform=True) as fused, _server(scene, warm_start=True) as copy:
+        for t in (30, 31, 32):
+            xf = scene.transforms(t)
+            pairs = scene.candidate_pairs(t, 8000)
+            a = _copy(fused.wait(fused.submit(fused.set_transforms(xf), pairs)))
+            c = _copy(copy.wait(copy.submit(copy.set_transforms(xf), pairs)))
+            posed = twin.pose_points(scene.counts, scene.local, xf)
+            b = _batch(scene, posed, pairs)
+            o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK_EPA, precision="f64",
+                        threads=16)
+            parity.assert_parity(parity.check(b, a, o, label=f"fused tick{t}"), max_witness_mismatch_frac=2e-3)
+            dp = float(np.abs(posed.astype(np.float64) - scene.world(xf)).max())
+            assert dp <= 1e-5
+            da, dc = a["dist"].astype(np.float64), c["dist"].astype(np.float64)
+            band = np.minimum(np.abs(da), np.abs(dc)) <= 2 * parity.BAND * parity.pair_scale(b) + 2 * dp
+            ca, cc = (a["status"] & 8) != 0, (c["status"] & 8) != 0
+            assert np.all((ca == cc) | band)
+            sep = ~ca & ~cc & ~band
+            assert np.all(np.abs(da[sep] - dc[sep]) <= 2 * parity.REL * np.abs(da[sep]) + 2 * dp)
+            con = ca & cc & ~band
+            assert np.all(np.abs(da[con] - dc[con]) <= 2 * parity.ABS4 + 2 * dp)
+
+
+def test_fused_transform_refuses_world_copy_uses(scene):
+    """A fused-transform server keeps no world copy: broad-phase requests and the world
+    layout are refused with OGX_ERR_INVALID, pair requests run."""
+    from ogx import _lib
+    with _server(scene, warm_start=False, fused_transform=True) as srv:
+        v = srv.set_transforms(scene.transforms(1))
+        with pytest.raises(_lib.OgxError):
+            srv.world_layout(v)
+        with pytest.raises(_lib.OgxError):
+            srv.submit_broadphase(v, cell=5.0, margin=0.5, max_pairs=1000)
+        assert srv.wait(srv.submit(v, scene.candidate_pairs(1, 100))).dist.shape == (100,)

@@ -40,3 +40,29 @@ def test_default_beats_reference_fp32_accuracy(orc, twin):
     e_ref = np.abs(o32["dist"][sep] - o64["dist"][sep]) / o64["dist"][sep]
     e_us = np.abs(r["dist"][sep] - o64["dist"][sep]) / o64["dist"][sep]
     assert e_us.max() <= 1e-5 < e_ref.max()
+
+
+def test_posed_pipeline_vs_oracle(orc, twin):
+    """The fused-transform pipeline (bodies in their own frame, each pose applied as the
+    points are read, support scans on the direction rotated into the body frame) against
+    the FP64 oracle on the same world points (pose_point of every body point), and
+    against the world-frame pipeline on those points."""
+    scene = W.serving_scene(seed=41, n_bodies=2000)
+    xf = scene.transforms(3)
+    pairs = scene.candidate_pairs(3, 6000)
+    world = twin.pose_points(scene.counts, scene.local, xf)
+    bw = W.Batch(world, scene.offsets, scene.counts, pairs, "serving")
+    bl = W.Batch(scene.local, scene.offsets, scene.counts, pairs, "serving")
+    o = orc.run(bw.coords, bw.offsets, bw.counts, bw.pairs, mode=orc.MODE_GJK_EPA, precision="f64", threads=8)
+    posed = twin.run(bl, xf=xf)
+    parity.assert_parity(parity.check(bw, posed, o, label="posed"), max_witness_mismatch_frac=2e-3)
+    plain = twin.run(bw)
+    assert np.array_equal(posed["dist"] < 0, plain["dist"] < 0)
+    close = np.abs(posed["dist"].astype(np.float64) - plain["dist"]) <= 1e-5 * np.maximum(1, np.abs(plain["dist"]))
+    assert close.all()
+    # the posed points themselves: R p + t within FP32 rounding of the FP64 product
+    body = np.repeat(np.arange(scene.n_bodies), scene.counts)
+    m = xf.astype(np.float64)[body]
+    p = scene.local.astype(np.float64)
+    exact = np.stack([(m[:, 3 * r:3 * r + 3] * p).sum(1) + m[:, 9 + r] for r in range(3)], axis=1)
+    assert np.abs(world - exact).max() <= 4e-7 * np.abs(exact).max()

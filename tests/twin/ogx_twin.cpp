@@ -28,6 +28,7 @@ struct Job {
   float* nrm;
   int32_t* status;
   int32_t* iters;
+  const float* xf;  // poses (12 floats per body) for the posed pipeline, or null
 };
 
 struct Work {
@@ -35,11 +36,17 @@ struct Work {
   EpaMemCert full;
 };
 
+void bind(MemBodies& B, const Job& J, int b1, int b2, BodyRef A, BodyRef Bb) { B.bind(J.pool, A, Bb); }
+void bind(Posed<MemBodies>& B, const Job& J, int b1, int b2, BodyRef A, BodyRef Bb) {
+  B.bind_posed(J.pool, A, Bb, J.xf + 12 * (size_t)b1, J.xf + 12 * (size_t)b2);
+}
+
+template <class Bodies>
 void one(const Job& J, int i, Work& M) {
   const int b1 = J.pairs[2 * i], b2 = J.pairs[2 * i + 1];
   BodyRef A{J.quad[b1], J.counts[b1]}, Bb{J.quad[b2], J.counts[b2]};
-  MemBodies B;
-  B.bind(J.pool, A, Bb);
+  Bodies B;
+  bind(B, J, b1, b2, A, Bb);
   SerialTeam t;
   GjkState g;
   gjk_pair(t, B, *J.cfg, g);
@@ -114,7 +121,12 @@ void one(const Job& J, int i, Work& M) {
 void* worker(void* arg) {
   const Job& J = *static_cast<const Job*>(arg);
   Work* M = new Work;
-  for (int i = J.lo; i < J.hi; ++i) one(J, i, *M);
+  for (int i = J.lo; i < J.hi; ++i) {
+    if (J.xf)
+      one<Posed<MemBodies>>(J, i, *M);
+    else
+      one<MemBodies>(J, i, *M);
+  }
   delete M;
   return nullptr;
 }
@@ -128,11 +140,26 @@ int twin_config(int reference, ogx_config* out) {
   return 0;
 }
 
-int twin_run(int npairs, const float* pool, const uint32_t* quad, const int32_t* counts,
-             const int32_t* pairs, int mode, const ogx_config* cfg, float* dist, gkSimplex* smp,
-             float* nrm, int32_t* status, int32_t* iters, int nthreads) {
+// posed points of every body (the fused-transform pipeline's world points): out and
+// local are xyz of all bodies concatenated, xf 12 floats per body
+int twin_pose_points(int nbodies, const int32_t* counts, const float* local, const float* xf, float* out) {
+  size_t k = 0;
+  for (int b = 0; b < nbodies; ++b)
+    for (int i = 0; i < counts[b]; ++i, ++k) {
+      const fv3 p = pose_point(xf + 12 * (size_t)b, v3<float>(local[3 * k], local[3 * k + 1], local[3 * k + 2]));
+      out[3 * k] = p.x;
+      out[3 * k + 1] = p.y;
+      out[3 * k + 2] = p.z;
+    }
+  return 0;
+}
+
+// xf: null, or poses (12 floats per body) to run the posed pipeline on the pool's bodies
+int twin_run_posed(int npairs, const float* pool, const uint32_t* quad, const int32_t* counts,
+                   const int32_t* pairs, int mode, const ogx_config* cfg, float* dist, gkSimplex* smp,
+                   float* nrm, int32_t* status, int32_t* iters, int nthreads, const float* xf) {
   if (npairs < 0 || (mode != 1 && mode != 2)) return -1;
-  Job base{0, npairs, mode, pool, quad, counts, pairs, cfg, dist, smp, nrm, status, iters};
+  Job base{0, npairs, mode, pool, quad, counts, pairs, cfg, dist, smp, nrm, status, iters, xf};
   if (nthreads <= 1 || npairs < 64) {
     worker(&base);
     return 0;
@@ -147,5 +174,12 @@ int twin_run(int npairs, const float* pool, const uint32_t* quad, const int32_t*
   }
   for (int k = 0; k < nthreads; ++k) pthread_join(th[k], nullptr);
   return 0;
+}
+
+int twin_run(int npairs, const float* pool, const uint32_t* quad, const int32_t* counts,
+             const int32_t* pairs, int mode, const ogx_config* cfg, float* dist, gkSimplex* smp,
+             float* nrm, int32_t* status, int32_t* iters, int nthreads) {
+  return twin_run_posed(npairs, pool, quad, counts, pairs, mode, cfg, dist, smp, nrm, status, iters, nthreads,
+                        nullptr);
 }
 }
