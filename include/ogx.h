@@ -345,6 +345,11 @@ typedef struct ogx_server_config {
   int world_slots;         /* world-space copies of the pool (transform versions kept) */
   int warm_start;          /* 1: warm-start GJK from the previous simplex of the pair */
   int warm_capacity_log2;  /* warm-start table entries (16 B each) */
+  int64_t max_bytes_in_flight; /* admission budget in bytes of device working memory of
+                            * the running requests (pairs, results, warm starts and the
+                            * pipeline's work lists: ogx_server_admission gives the bytes
+                            * per pair); 0: half the device memory free once the server's
+                            * buffers are allocated */
   int fused_transform;     /* 1: no world copies; the GJK/EPA kernels apply each body's
                             * pose as they read its points (world point R p + t in FP32,
                             * one fused multiply-add chain per coordinate; support scans
@@ -400,6 +405,12 @@ ogx_status ogx_server_wait(ogx_server* server, int64_t ticket, double timeout_s,
 ogx_status ogx_server_wait_phases(ogx_server* server, int64_t ticket, double timeout_s, double* latency_ms,
                                   double* phases_ms);
 /* Device layout of the world-space pool of a version (for checks and custom kernels). */
+/* The admission budgets of a server: a request is admitted, oldest first, when a slot is
+ * free and both the pairs and the device bytes in flight (pairs x bytes_per_pair) stay
+ * within their budgets (or nothing else is running); peak_bytes = the most device bytes
+ * in flight so far.  Any pointer may be NULL. */
+ogx_status ogx_server_admission(ogx_server* server, int64_t* max_pairs, int64_t* max_bytes,
+                                int64_t* bytes_per_pair, int64_t* peak_bytes);
 ogx_status ogx_server_world_layout(ogx_server* server, int64_t version, float** d_points,
                                    void** d_bodies);
 

@@ -477,6 +477,10 @@ extern "C" int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap) {
   return kCntSlots;
 }
 
+size_t ogx_scratch_bytes_per_pair() {
+  return 2 * kBuckets * sizeof(int) + sizeof(PolishRec) + sizeof(RefineRec) + 2 * sizeof(int);
+}
+
 ogx_status ogx_ctx::ensure_scratch(int npairs) {
   if ((size_t)npairs <= cap_pairs && d_counts) return OGX_OK;
   cudaStreamSynchronize(stream);

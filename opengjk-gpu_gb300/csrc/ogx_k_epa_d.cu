@@ -3,7 +3,9 @@
 // lanes per pair, capped at 128 registers (4 blocks of 4 warps per SM, which the working
 // sets and the slots together still fit).  Measured slower than the register-loaded
 // scans on the GB300 (the autotuner keeps those); compiled so that it can pick these
-// where the balance between load latency and instruction count differs.
+// where the balance between load latency and instruction count differs.  (EPA variants
+// with the GJK kernels' four-blocks-in-flight scan at 128 registers were never picked by
+// the autotuner on the 1M-pair power-law step and are not compiled.)
 #include "ogx_kernels.cuh"
 
 namespace ogx {

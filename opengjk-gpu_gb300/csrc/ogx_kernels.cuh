@@ -364,7 +364,7 @@ struct KernelInfo {
 constexpr int kOccShift = 8;
 constexpr int kStageShift = 16;
 OGX_HD int variant_blocks(int K) { return K & ((1 << kOccShift) - 1); }
-OGX_HD int variant_stages(int K) { return K >> kStageShift; }
+OGX_HD int variant_stages(int K) { return (K >> kStageShift) & 0xff; }
 
 // Compiled variants of the bucket kernels (ogx_k_gjk_*.cu / ogx_k_epa_*.cu).  A variant
 // (L, K) can serve a bucket whose bodies have at most 4 L K points (K = 0: any size, the

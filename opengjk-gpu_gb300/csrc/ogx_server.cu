@@ -11,8 +11,9 @@
 //    only and the GJK/EPA kernels apply them as they read the points (posed kernels);
 //  * requests (a pair list of one tick) are queued; a scheduler thread admits the oldest
 //    queued request as soon as a slot (stream + device buffers for `slot_pairs` pairs) is
-//    free and the pairs in flight stay within `max_pairs_in_flight`; admitted requests
-//    run concurrently on their slots' streams;
+//    free and the pairs in flight stay within `max_pairs_in_flight` and their device
+//    working memory within `max_bytes_in_flight`; admitted requests run concurrently on
+//    their slots' streams;
 //  * each slot's pipeline: pairs host->device, warm-start lookup, GJK + EPA (the engine's
 //    kernels), warm-start store, results device->host, one event; the scheduler copies the
 //    results out when the event completes and frees the slot;
@@ -215,6 +216,9 @@ struct ogx_server {
   std::unordered_map<int64_t, Request*> reqs;
   int64_t next_id = 1;
   int64_t pairs_in_flight = 0;
+  int64_t bytes_per_pair = 0;  // device working memory of one pair of a request
+  int64_t max_bytes = 0;       // admission budget in device bytes
+  int64_t peak_bytes = 0;
   bool stop = false;
   std::thread sched;
 
@@ -406,7 +410,11 @@ void ogx_server::loop() {
     while (!queue.empty()) {
       Request* r = queue.front();
       const int want = r->broad ? std::min(r->max_pairs, sc.slot_pairs) : r->npairs;
-      if (pairs_in_flight + want > sc.max_pairs_in_flight && pairs_in_flight > 0) break;
+      // admission by the pairs and the device memory in flight (a request that exceeds a
+      // budget alone still runs once nothing else does)
+      if (pairs_in_flight > 0 && (pairs_in_flight + want > sc.max_pairs_in_flight ||
+                                  (pairs_in_flight + want) * bytes_per_pair > max_bytes))
+        break;
       Slot* free_slot = nullptr;
       for (Slot& s : slots)
         if (!s.req) {
@@ -435,6 +443,7 @@ void ogx_server::loop() {
       }
       free_slot->reserved = want;
       pairs_in_flight += want;
+      peak_bytes = std::max(peak_bytes, pairs_in_flight * bytes_per_pair);
       world_refs[w] += 1;
       progress = true;
     }
@@ -502,6 +511,7 @@ extern "C" void ogx_server_config_default(ogx_server_config* sc) {
   sc->world_slots = 4;
   sc->warm_start = 1;
   sc->warm_capacity_log2 = 22;
+  sc->max_bytes_in_flight = 0;
   sc->fused_transform = 0;
 }
 
@@ -515,7 +525,7 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
   if (scfg) sc = *scfg;
   if (sc.slots < 1 || sc.slots > 64 || sc.slot_pairs < 1 || sc.world_slots < 2 || sc.world_slots > 64 ||
       sc.max_pairs_in_flight < sc.slot_pairs || sc.warm_capacity_log2 < 10 || sc.warm_capacity_log2 > 30 ||
-      sc.fused_transform < 0 || sc.fused_transform > 1)
+      sc.fused_transform < 0 || sc.fused_transform > 1 || sc.max_bytes_in_flight < 0)
     return ogx_fail(OGX_ERR_INVALID, "server config out of range");
   ogx_server* S = new ogx_server();
   S->sc = sc;
@@ -588,6 +598,19 @@ extern "C" ogx_status ogx_server_create(int device, const ogx_config* cfg, const
   if (!st) {
     S->grid_aux = 4 * S->pctx->sm_count;
     if ((e = cudaStreamSynchronize(S->pctx->stream)) != cudaSuccess) st = ogx_cuda_fail(e, "server setup");
+  }
+  if (!st) {
+    // a request's device working memory per pair: its pairs, results and warm-start
+    // entries, and the pipeline's work lists (sized 1.25 x the pairs)
+    S->bytes_per_pair = (int64_t)(sizeof(gkCollisionPair) + sizeof(gkSimplex) + 4 * sizeof(float) +
+                                  sizeof(int32_t) + sizeof(int2)) +
+                        (int64_t)(5 * ogx_scratch_bytes_per_pair()) / 4;
+    S->max_bytes = sc.max_bytes_in_flight;
+    if (S->max_bytes == 0) {
+      size_t free_b = 0, total_b = 0;
+      if ((e = cudaMemGetInfo(&free_b, &total_b)) != cudaSuccess) st = ogx_cuda_fail(e, "server memory info");
+      S->max_bytes = (int64_t)(free_b / 2);
+    }
   }
   if (st) {
     S->release();
@@ -805,6 +828,17 @@ extern "C" ogx_status ogx_server_poll(ogx_server* S, int64_t ticket, int* done) 
   auto it = S->reqs.find(ticket);
   if (it == S->reqs.end()) return ogx_fail(OGX_ERR_INVALID, "unknown ticket %lld", (long long)ticket);
   *done = it->second->state >= 2;
+  return OGX_OK;
+}
+
+extern "C" ogx_status ogx_server_admission(ogx_server* S, int64_t* max_pairs, int64_t* max_bytes,
+                                           int64_t* bytes_per_pair, int64_t* peak_bytes) {
+  if (!S) return ogx_fail(OGX_ERR_INVALID, "NULL server");
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (max_pairs) *max_pairs = S->sc.max_pairs_in_flight;
+  if (max_bytes) *max_bytes = S->max_bytes;
+  if (bytes_per_pair) *bytes_per_pair = S->bytes_per_pair;
+  if (peak_bytes) *peak_bytes = S->peak_bytes;
   return OGX_OK;
 }
 

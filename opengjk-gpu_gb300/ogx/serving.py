@@ -19,7 +19,7 @@ P = ctypes.c_void_p
 class ServerConfig(ctypes.Structure):
     _fields_ = [("slots", ctypes.c_int), ("slot_pairs", ctypes.c_int), ("max_pairs_in_flight", ctypes.c_int),
                 ("world_slots", ctypes.c_int), ("warm_start", ctypes.c_int), ("warm_capacity_log2", ctypes.c_int),
-                ("fused_transform", ctypes.c_int)]
+                ("max_bytes_in_flight", ctypes.c_int64), ("fused_transform", ctypes.c_int)]
 
 
 def _bind(lib):
@@ -46,6 +46,8 @@ def _bind(lib):
     lib.ogx_server_wait_phases.restype = ctypes.c_int
     lib.ogx_server_wait_phases.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double)]
+    lib.ogx_server_admission.restype = ctypes.c_int
+    lib.ogx_server_admission.argtypes = [P] + [ctypes.POINTER(I64)] * 4
     lib.ogx_server_world_layout.restype = ctypes.c_int
     lib.ogx_server_world_layout.argtypes = [P, I64, ctypes.POINTER(P), ctypes.POINTER(P)]
     lib._ogx_server_bound = True
@@ -137,10 +139,11 @@ class Server:
     def __init__(self, counts, local_xyz, config: _lib.Config | None = None, device: int = 0, slots: int = 4,
                  slot_pairs: int = 262144, max_pairs_in_flight: int = 1 << 20, world_slots: int = 4,
                  warm_start: bool = True, warm_capacity_log2: int = 22, result_sets: int | None = None,
-                 fused_transform: bool = False):
+                 fused_transform: bool = False, max_bytes_in_flight: int = 0):
         """`result_sets` page-locked result sets of `slot_pairs` pairs are allocated up
         front (default 2 x slots) and recycled by Request.release().  `fused_transform`:
-        keep no world copies, the kernels apply the poses as they read the points."""
+        keep no world copies, the kernels apply the poses as they read the points.
+        `max_bytes_in_flight`: admission budget in device bytes (0: half the free memory)."""
         self.lib = _lib.load()
         _bind(self.lib)
         sc = ServerConfig()
@@ -148,6 +151,7 @@ class Server:
         sc.slots, sc.slot_pairs, sc.max_pairs_in_flight = slots, slot_pairs, max_pairs_in_flight
         sc.world_slots, sc.warm_start, sc.warm_capacity_log2 = world_slots, int(warm_start), warm_capacity_log2
         sc.fused_transform = int(fused_transform)
+        sc.max_bytes_in_flight = int(max_bytes_in_flight)
         self.counts = np.ascontiguousarray(counts, np.int32)
         local = np.ascontiguousarray(local_xyz, np.float32)
         h = P()
@@ -227,6 +231,13 @@ class Server:
         req.latency_ms = lat.value
         req.phases_ms = tuple(ph)
         return req
+
+    def admission(self) -> dict:
+        """Admission budgets (pairs, device bytes), bytes per pair, peak bytes in flight."""
+        v = [ctypes.c_int64() for _ in range(4)]
+        _lib.check(self.lib.ogx_server_admission(self.handle, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("max_pairs_in_flight", "max_bytes_in_flight", "bytes_per_pair", "peak_bytes_in_flight"),
+                        (x.value for x in v)))
 
     def world_layout(self, version: int):
         pts, bodies = P(), P()

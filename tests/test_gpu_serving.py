@@ -351,3 +351,27 @@ def test_fused_transform_refuses_world_copy_uses(scene):
         with pytest.raises(_lib.OgxError):
             srv.submit_broadphase(v, cell=5.0, margin=0.5, max_pairs=1000)
         assert srv.wait(srv.submit(v, scene.candidate_pairs(1, 100))).dist.shape == (100,)
+
+
+def test_admission_by_device_memory(scene):
+    """Requests are admitted by device memory: with a byte budget of one and a half
+    requests' working memory, requests run one at a time (the peak bytes in flight is one
+    request's), and each result equals the same request run alone.  Without a budget the
+    server derives one from the free device memory."""
+    n = 10000
+    with _server(scene, warm_start=False) as srv:
+        adm = srv.admission()
+        assert adm["bytes_per_pair"] > 200 and adm["max_bytes_in_flight"] > 10 * n * adm["bytes_per_pair"]
+        v = srv.set_transforms(scene.transforms(2))
+        pairs = [scene.candidate_pairs(2, n)[np.random.default_rng(k).permutation(n)] for k in range(4)]
+        alone = [_copy(srv.wait(srv.submit(v, p))) for p in pairs]
+    budget = int(1.5 * n * adm["bytes_per_pair"])
+    with _server(scene, warm_start=False, max_bytes_in_flight=budget) as srv:
+        v = srv.set_transforms(scene.transforms(2))
+        reqs = [srv.submit(v, p) for p in pairs]
+        got = [_copy(srv.wait(r)) for r in reqs]
+        adm2 = srv.admission()
+    assert adm2["max_bytes_in_flight"] == budget
+    assert adm2["peak_bytes_in_flight"] == n * adm["bytes_per_pair"]
+    for a, g in zip(alone, got):
+        assert np.array_equal(a["dist"], g["dist"]) and np.array_equal(a["normal"], g["normal"])
