@@ -17,6 +17,8 @@
 //  * contact_normals may be NULL where the reference documents it as nullable
 //    (examples/gpu/example.h:39) -- the reference writes through it regardless.
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <string.h>
 
 #include <algorithm>
@@ -225,6 +227,9 @@ struct Compat {
   size_t c64_cap = 0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   float last_ms = 0.0f;
+  // page-locked staging of the results of host-buffer calls into pageable caller arrays
+  char* h_res = nullptr;
+  size_t h_res_bytes = 0;
 };
 
 constexpr int kMaxDevices = 16;
@@ -243,6 +248,42 @@ ogx_status grow(T** p, size_t* cap, size_t need, const char* what) {
   if (e != cudaSuccess) return ogx_cuda_fail(e, what);
   *cap = n;
   return OGX_OK;
+}
+
+// Host copy of `bytes` bytes on up to 16 threads (one for small copies).
+void parallel_copy(void* dst, const void* src, size_t bytes) {
+  const int nt = (int)std::min<size_t>(16, std::max<size_t>(1, bytes >> 22));
+  if (nt == 1) {
+    memcpy(dst, src, bytes);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int k = 0; k < nt; ++k)
+    th.emplace_back([=] {
+      const size_t a = bytes * k / nt, b = bytes * (k + 1) / nt;
+      memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, b - a);
+    });
+  for (auto& t : th) t.join();
+}
+
+// fn(lo, hi, k) over [0, n) in nt contiguous pieces, piece k on its own thread (the
+// caller's thread takes piece 0)
+template <class F>
+void parallel_for(int n, int nt, F fn) {
+  std::vector<std::thread> th;
+  for (int k = 1; k < nt; ++k)
+    th.emplace_back([&, k] { fn((int)((int64_t)n * k / nt), (int)((int64_t)n * (k + 1) / nt), k); });
+  fn(0, (int)((int64_t)n / nt), 0);
+  for (auto& t : th) t.join();
+}
+
+bool is_pinned(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
 }
 
 // A context leased for the duration of one call; back on its device's free list after.
@@ -320,21 +361,50 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
   std::vector<const float*> src(nb);
   std::vector<int64_t> voff(nb);
   std::vector<BodyRef> refs(nb);
-  int64_t pts = 0;
-  uint64_t quad = 0;
-  for (int i = 0; i < nb; ++i) {
-    const gkPolytope& p = b ? ((i & 1) ? b[i >> 1] : a[i >> 1]) : a[i];
-    if (p.numpoints < 1 || !p.coord)
-      return ogx_fail(OGX_ERR_INVALID, "polytope %d: numpoints %d, coord %p", i, p.numpoints, (void*)p.coord);
-    counts[i] = p.numpoints;
-    src[i] = p.coord;
-    voff[i] = pts;
-    refs[i].quad = (uint32_t)quad;
-    refs[i].n = p.numpoints;
-    pts += p.numpoints;
-    quad += 3 * (uint64_t)((p.numpoints + 3) / 4);
-    if (quad >= (1ull << 32)) return ogx_fail(OGX_ERR_CAPACITY, "pool exceeds 2^32 float4 blocks");
+  // body table in two parallel passes over pieces of the descriptors: per piece the
+  // point and float4-block totals (and the first invalid descriptor), then, after a
+  // prefix over the pieces, every body's offsets
+  const int nt = (int)std::min<int64_t>(16, std::max<int64_t>(1, nb >> 15));
+  std::vector<int64_t> piece_pts(nt + 1, 0), piece_quad(nt + 1, 0);
+  std::vector<int> bad(nt, -1);
+  parallel_for(nb, nt, [&](int lo, int hi, int k) {
+    int64_t np = 0, nq = 0;
+    for (int i = lo; i < hi; ++i) {
+      const gkPolytope& p = b ? ((i & 1) ? b[i >> 1] : a[i >> 1]) : a[i];
+      if (p.numpoints < 1 || !p.coord) {
+        bad[k] = i;
+        return;
+      }
+      counts[i] = p.numpoints;
+      src[i] = p.coord;
+      np += p.numpoints;
+      nq += 3 * (int64_t)((p.numpoints + 3) / 4);
+    }
+    piece_pts[k + 1] = np;
+    piece_quad[k + 1] = nq;
+  });
+  for (int k = 0; k < nt; ++k)
+    if (bad[k] >= 0) {
+      const gkPolytope& p = b ? ((bad[k] & 1) ? b[bad[k] >> 1] : a[bad[k] >> 1]) : a[bad[k]];
+      return ogx_fail(OGX_ERR_INVALID, "polytope %d: numpoints %d, coord %p", bad[k], p.numpoints, (void*)p.coord);
+    }
+  for (int k = 0; k < nt; ++k) {
+    piece_pts[k + 1] += piece_pts[k];
+    piece_quad[k + 1] += piece_quad[k];
   }
+  const int64_t pts = piece_pts[nt];
+  const uint64_t quad = (uint64_t)piece_quad[nt];
+  if (quad >= (1ull << 32)) return ogx_fail(OGX_ERR_CAPACITY, "pool exceeds 2^32 float4 blocks");
+  parallel_for(nb, nt, [&](int lo, int hi, int k) {
+    int64_t np = piece_pts[k], nq = piece_quad[k];
+    for (int i = lo; i < hi; ++i) {
+      voff[i] = np;
+      refs[i].quad = (uint32_t)nq;
+      refs[i].n = counts[i];
+      np += counts[i];
+      nq += 3 * (int64_t)((counts[i] + 3) / 4);
+    }
+  });
   ogx_ctx* ctx = c.ctx;
   cudaStream_t st = ctx->stream;
   const size_t bytes = (size_t)pts * 3 * sizeof(float);
@@ -345,18 +415,37 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
   if (s) return s;
   cudaStreamSynchronize(st);  // staging buffers may still be read by a previous call
   char* h = static_cast<char*>(ctx->h_stage);
-  // gather all coordinates (parallel for large batches)
-  const int nt = (int)std::min<int64_t>(16, std::max<int64_t>(1, pts >> 18));
+  // Gather the coordinates into the pinned staging in pieces of bodies, on up to 16
+  // threads, and upload each piece as soon as it is gathered: the copy engine moves piece
+  // k while the threads gather piece k + 1.
+  const int gt = (int)std::min<int64_t>(16, std::max<int64_t>(1, pts >> 18));
+  const int pieces = bytes >= ((size_t)64 << 20) ? 8 : 1;
+  std::vector<std::atomic<int>> gathered(pieces);
+  for (auto& g : gathered) g.store(0);
+  auto piece_begin = [&](int pc) { return (int)((int64_t)nb * pc / pieces); };
   std::vector<std::thread> th;
-  for (int k = 0; k < nt; ++k)
+  for (int k = 1; k < gt; ++k)
     th.emplace_back([&, k] {
-      for (int i = (int)((int64_t)nb * k / nt); i < (int)((int64_t)nb * (k + 1) / nt); ++i)
-        memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
+      for (int pc = 0; pc < pieces; ++pc) {
+        const int i0 = piece_begin(pc), i1 = piece_begin(pc + 1);
+        for (int i = (int)(i0 + (int64_t)(i1 - i0) * k / gt); i < (int)(i0 + (int64_t)(i1 - i0) * (k + 1) / gt); ++i)
+          memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
+        gathered[pc].fetch_add(1);
+      }
     });
+  cudaError_t e = cudaSuccess;
+  for (int pc = 0; pc < pieces; ++pc) {
+    const int i0 = piece_begin(pc), i1 = piece_begin(pc + 1);
+    for (int i = i0; i < (int)(i0 + (int64_t)(i1 - i0) / gt); ++i)  // this thread's share
+      memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
+    while (gathered[pc].load() < gt - 1) std::this_thread::yield();
+    const size_t b0 = (size_t)voff[i0] * 12, b1 = i1 < nb ? (size_t)voff[i1] * 12 : bytes;
+    if (e == cudaSuccess && b1 > b0)
+      e = cudaMemcpyAsync(static_cast<char*>(ctx->d_stage) + b0, h + b0, b1 - b0, cudaMemcpyHostToDevice, st);
+  }
   for (auto& t : th) t.join();
   memcpy(h + bytes, refs.data(), nb * sizeof(BodyRef));
   memcpy(h + bytes + nb * sizeof(BodyRef), voff.data(), nb * sizeof(int64_t));
-  cudaError_t e = cudaMemcpyAsync(ctx->d_stage, h, bytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(c.d_bodies, h + bytes, nb * sizeof(BodyRef), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
@@ -438,10 +527,18 @@ ogx_status host_query(const gkPolytope* a, const gkPolytope* b, int nbodies, int
   if (a64) e = cudaMemcpyAsync(c->d_c64, c64.data(), c64.size() * sizeof(double), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "double coordinate upload");
   if (host_pairs) {
-    for (int i = 0; i < npairs; ++i)
-      if (host_pairs[i].idx1 < 0 || host_pairs[i].idx1 >= nbodies || host_pairs[i].idx2 < 0 ||
-          host_pairs[i].idx2 >= nbodies)
-        return ogx_fail(OGX_ERR_INVALID, "pair %d: index out of range", i);
+    const int nt = (int)std::min<int64_t>(16, std::max<int64_t>(1, npairs >> 16));
+    std::vector<int> bad(nt, -1);
+    parallel_for(npairs, nt, [&](int lo, int hi, int k) {
+      for (int i = lo; i < hi; ++i)
+        if (host_pairs[i].idx1 < 0 || host_pairs[i].idx1 >= nbodies || host_pairs[i].idx2 < 0 ||
+            host_pairs[i].idx2 >= nbodies) {
+          bad[k] = i;
+          return;
+        }
+    });
+    for (int k = 0; k < nt; ++k)
+      if (bad[k] >= 0) return ogx_fail(OGX_ERR_INVALID, "pair %d: index out of range", bad[k]);
     e = cudaMemcpyAsync(c->d_pairs, host_pairs, npairs * sizeof(gkCollisionPair), cudaMemcpyHostToDevice, st);
   } else {
     k_pairs_iota<<<std::min(1024, (npairs + 255) / 256), 256, 0, st>>>(c->d_pairs, npairs);
@@ -454,13 +551,35 @@ ogx_status host_query(const gkPolytope* a, const gkPolytope* b, int nbodies, int
   if (e != cudaSuccess) return ogx_cuda_fail(e, "input upload");
   s = run_timed(*c, nbodies, npairs, c->d_pairs, c->d_smp, c->d_dist, c->d_nrm, mode, a64 != nullptr);
   if (s) return s;
-  e = cudaMemcpyAsync(smp, c->d_smp, npairs * sizeof(gkSimplex), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dist, c->d_dist, npairs * sizeof(float), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess && nrm && mode != kModeGjk)
-    e = cudaMemcpyAsync(nrm, c->d_nrm, 3 * (size_t)npairs * sizeof(float), cudaMemcpyDeviceToHost, st);
+  // Results: straight into page-locked caller arrays; pageable ones through the pinned
+  // staging (a full-rate copy) and a parallel host copy.
+  const bool want_nrm = nrm && mode != kModeGjk;
+  const size_t sb = npairs * sizeof(gkSimplex), db = npairs * sizeof(float), nbytes = 3 * db;
+  const bool direct = is_pinned(smp) && is_pinned(dist) && (!want_nrm || is_pinned(nrm));
+  char* hs = nullptr;
+  if (!direct) {
+    const size_t need = sb + db + (want_nrm ? nbytes : 0);
+    if (need > c->h_res_bytes) {
+      if (c->h_res) cudaFreeHost(c->h_res);
+      c->h_res = nullptr;
+      c->h_res_bytes = 0;
+      if ((e = cudaMallocHost(&c->h_res, need)) != cudaSuccess) return ogx_cuda_fail(e, "pinned result staging");
+      c->h_res_bytes = need;
+    }
+    hs = c->h_res;
+  }
+  e = cudaMemcpyAsync(direct ? (void*)smp : hs, c->d_smp, sb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(direct ? (void*)dist : hs + sb, c->d_dist, db, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && want_nrm)
+    e = cudaMemcpyAsync(direct ? (void*)nrm : hs + sb + db, c->d_nrm, nbytes, cudaMemcpyDeviceToHost, st);
   if (e != cudaSuccess) return ogx_cuda_fail(e, "result copy");
   s = finish(*c);
   if (s) return s;
+  if (!direct) {
+    parallel_copy(smp, hs, sb);
+    parallel_copy(dist, hs + sb, db);
+    if (want_nrm) parallel_copy(nrm, hs + sb + db, nbytes);
+  }
   if (w1 || w2) {
     for (int i = 0; i < npairs; ++i)
       for (int k = 0; k < 3; ++k) {
