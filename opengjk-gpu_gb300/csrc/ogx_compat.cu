@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -160,6 +161,35 @@ __global__ void k_desc_pack(DescSrc src, int nb, BodyRef* __restrict__ bodies, f
   }
 }
 
+// Pack from a table of coordinate pointers (one per body, xyz interleaved) that address
+// the caller's host arrays: on a device that reads pageable host memory through the host's
+// page tables (cudaDevAttrPageableMemoryAccess, the GPU of a Grace system over NVLink-C2C)
+// the kernel loads the points where the caller keeps them, so the host gathers nothing.
+// Bodies with a NaN or infinite coordinate are marked as k_pack does.
+__global__ void k_pack_ptrs(const float* const* __restrict__ src, int nb, BodyRef* __restrict__ bodies,
+                            float* __restrict__ pool) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int b = warp; b < nb; b += nwarps) {
+    const BodyRef r = bodies[b];
+    const float* c = src[b];
+    const int n4 = round4(r.n);
+    float* dst = pool + 4 * (size_t)r.quad;
+    bool finite = true;
+    for (int i = lane; i < n4; i += 32) {
+      const int s = i < r.n ? i : 0;
+      const float x = c[3 * s], y = c[3 * s + 1], z = c[3 * s + 2];
+      finite = finite && is_finite(x) && is_finite(y) && is_finite(z);
+      dst[i] = x;
+      dst[n4 + i] = y;
+      dst[2 * n4 + i] = z;
+    }
+    finite = __all_sync(0xffffffffu, finite);
+    if (lane == 0 && !finite) bodies[b].n = -r.n;
+  }
+}
+
 // Bodies given in double (the *_f64 calls): every separated pair continues GJK in FP64 on
 // the caller's double points from the FP32 pass's final simplex -- exact supports and
 // exact Minkowski points, one thread per pair -- so its distance carries no rounding of
@@ -225,6 +255,8 @@ struct Compat {
   size_t nrm_cap = 0;
   double* d_c64 = nullptr;  // the *_f64 calls: the bodies' double coordinates, pool order
   size_t c64_cap = 0;
+  const float** d_src = nullptr;  // per body: the caller's coordinate pointer (k_pack_ptrs)
+  size_t src_cap = 0;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   float last_ms = 0.0f;
   // page-locked staging of the results of host-buffer calls into pageable caller arrays
@@ -275,6 +307,27 @@ void parallel_for(int n, int nt, F fn) {
     th.emplace_back([&, k] { fn((int)((int64_t)n * k / nt), (int)((int64_t)n * (k + 1) / nt), k); });
   fn(0, (int)((int64_t)n / nt), 0);
   for (auto& t : th) t.join();
+}
+
+// Does the device read pageable host memory directly (through the host's page tables)?
+// Then host-buffer calls pack the caller's points on the device (k_pack_ptrs) instead of
+// gathering them on the host.  OGX_COMPAT_GATHER=1 in the environment forces the gather.
+bool pageable_reads(int dev) {
+  static std::atomic<int> known[kMaxDevices];  // 0 unknown, 1 no, 2 yes
+  if (dev < 0 || dev >= kMaxDevices) return false;
+  const char* force = std::getenv("OGX_COMPAT_GATHER");
+  if (force && force[0] == '1') return false;
+  int k = known[dev].load();
+  if (k == 0) {
+    int a = 0, t = 0;
+    const bool ok = cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+                    cudaDeviceGetAttribute(&t, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+                        cudaSuccess;
+    if (!ok) cudaGetLastError();
+    k = ok && a == 1 && t == 1 ? 2 : 1;
+    known[dev].store(k);
+  }
+  return k == 2;
 }
 
 bool is_pinned(const void* p) {
@@ -408,6 +461,31 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
   ogx_ctx* ctx = c.ctx;
   cudaStream_t st = ctx->stream;
   const size_t bytes = (size_t)pts * 3 * sizeof(float);
+  if (pageable_reads(ctx->device)) {
+    // the body table and the coordinate pointers up, the points packed from where the
+    // caller keeps them
+    const size_t tb = nb * sizeof(BodyRef), pb = nb * sizeof(const float*), ob = nb * sizeof(int64_t);
+    ogx_status s = ctx->ensure_stage(tb + pb + ob, 0);
+    if (!s) s = grow(&c.d_bodies, &c.bodies_cap, (size_t)nb, "compat body table");
+    if (!s) s = grow(&c.d_src, &c.src_cap, (size_t)nb, "compat coordinate pointers");
+    if (!s) s = grow(&c.d_voff, &c.voff_cap, (size_t)nb, "compat offsets");
+    if (!s) s = grow(&c.d_points, &c.points_cap, 4 * (size_t)quad + 4, "compat pool");
+    if (s) return s;
+    cudaStreamSynchronize(st);  // staging buffers may still be read by a previous call
+    char* h = static_cast<char*>(ctx->h_stage);
+    parallel_copy(h, refs.data(), tb);
+    parallel_copy(h + tb, src.data(), pb);
+    parallel_copy(h + tb + pb, voff.data(), ob);
+    cudaError_t e = cudaMemcpyAsync(c.d_bodies, h, tb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_src, h + tb, pb, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_voff, h + tb + pb, ob, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      k_pack_ptrs<<<8 * ctx->sm_count, 256, 0, st>>>(c.d_src, nb, c.d_bodies, c.d_points);
+      e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "polytope pack from host memory");
+    return OGX_OK;
+  }
   ogx_status s = ctx->ensure_stage(bytes + nb * (sizeof(BodyRef) + sizeof(int64_t)), bytes);
   if (!s) s = grow(&c.d_bodies, &c.bodies_cap, (size_t)nb, "compat body table");
   if (!s) s = grow(&c.d_voff, &c.voff_cap, (size_t)nb, "compat offsets");
@@ -552,7 +630,9 @@ ogx_status host_query(const gkPolytope* a, const gkPolytope* b, int nbodies, int
   s = run_timed(*c, nbodies, npairs, c->d_pairs, c->d_smp, c->d_dist, c->d_nrm, mode, a64 != nullptr);
   if (s) return s;
   // Results: straight into page-locked caller arrays; pageable ones through the pinned
-  // staging (a full-rate copy) and a parallel host copy.
+  // staging (a full-rate copy) and a parallel host copy.  (Writing pageable arrays from
+  // a copy kernel, where the device can, measured slower: a caller's fresh result arrays
+  // are first touched by the device, and the page faults are taken on its side.)
   const bool want_nrm = nrm && mode != kModeGjk;
   const size_t sb = npairs * sizeof(gkSimplex), db = npairs * sizeof(float), nbytes = 3 * db;
   const bool direct = is_pinned(smp) && is_pinned(dist) && (!want_nrm || is_pinned(nrm));

@@ -10,6 +10,8 @@ static const KernelInfo kVar[] = {
     {k_epa<4, 1, 5>, 4, 1 + (5 << kOccShift)}, {k_epa<8, 1, 5>, 8, 1 + (5 << kOccShift)},
     {k_epa<8, 2, 5>, 8, 2 + (5 << kOccShift)}, {k_epa<8, 0, 5>, 8, 5 << kOccShift},
     {k_epa<16, 0, 5>, 16, 5 << kOccShift},
+    // two register blocks at 128 registers (4 blocks per SM; the 96-register build spills)
+    {k_epa<8, 2, 4>, 8, 2 + (4 << kOccShift)},
 };
 
 int epa_variants_c(const KernelInfo** out) {

@@ -72,7 +72,7 @@ def _variant_columns(ctx):
     for kind in ("gjk", "epa"):
         for b in range(7):
             for L in (1, 2, 4, 8, 16, 32):
-                for K in (0, 1, 2, 4, 4 << 8, 5 << 8, 1 + (5 << 8), 2 + (5 << 8),
+                for K in (0, 1, 2, 4, 4 << 8, 5 << 8, 1 + (5 << 8), 2 + (5 << 8), 2 + (4 << 8),
                           (4 << 8) + (2 << 16), (4 << 8) + (3 << 16), (4 << 8) + (4 << 16),
                           (4 << 8) + (8 << 16)):
                     try:

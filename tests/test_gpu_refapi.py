@@ -123,3 +123,26 @@ def test_empty_and_invalid(engine):
     rc = L.ogx_compute_minimum_distance(1, bad[:1].ctypes.data, bad[1:].ctypes.data, smp.ctypes.data,
                                         dist.ctypes.data)
     assert rc == -1 and b"numpoints" in L.ogx_last_error()
+
+
+def test_host_calls_pack_in_place_or_gathered_alike(engine, monkeypatch):
+    """Host-buffer calls build the pool either on the device straight from the caller's
+    arrays (devices that read pageable host memory) or from a host gather into pinned
+    staging (OGX_COMPAT_GATHER=1, and every other device): the same bits, non-finite
+    bodies flagged either way."""
+    b = W.powerlaw(seed=44, n_pairs=4000)
+    coords = b.coords.copy()
+    coords[b.offsets[7] + 2, 1] = np.nan  # body 7: pair 3 is bad input
+    b = W.Batch(coords, b.offsets, b.counts, b.pairs, b.name)
+    bd1, bd2, pool = refapi.from_batch(b)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("OGX_COMPAT_GATHER", mode)
+        smp, dist, nrm = refapi.compute_gjk_epa(bd1, bd2)
+        smp_i, dist_i, nrm_i = refapi.compute_gjk_epa_indexed(pool, np.ascontiguousarray(b.pairs))
+        out[mode] = (smp.tobytes(), dist.copy(), nrm.copy(), smp_i.tobytes(), dist_i.copy())
+    a, g = out["0"], out["1"]
+    assert a[0] == g[0] and a[3] == g[3]
+    for x, y in ((a[1], g[1]), (a[2], g[2]), (a[4], g[4])):
+        assert np.array_equal(x, y, equal_nan=True)
+    assert np.isnan(a[1][3]) and np.isfinite(np.delete(a[1], 3)).all()
