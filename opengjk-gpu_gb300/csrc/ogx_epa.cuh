@@ -289,8 +289,9 @@ OGX_HD int tri_weights(fv3 p0, fv3 p1, fv3 p2, float* l) {
 // used, so that w0 - w1 = depth * normal holds.
 template <class Mem, class Bodies>
 // With rerun_ok, returns true when the origin's projection leaves the closest face
-// towards a neighbour that is not coplanar with it in FP64: nothing is emitted then and
-// the caller runs the contact again with FP64 planes.  Without (the FP64-plane pass
+// towards a neighbour more than 1e-5 rad off its plane (sine from the cross product of the
+// two FP32 normals, kEpaHopSin2): nothing is emitted then and the caller runs the contact
+// again with FP64 planes.  Without (the FP64-plane pass
 // itself, whose closest face is picked on the planes rounded to float, so two faces a
 // rounding apart can swap), the result comes from that near-coplanar neighbour, which
 // holds the projection.
