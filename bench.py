@@ -453,6 +453,12 @@ def serving_report(device: int, seed: int = 77, slots: int = 4, max_in_flight: i
         lat_mix, thr_mix = run(list(range(n_lists)), mix_rate, 300, seed + 1)
         big_rate = 0.5 * cap_big_hz
         lat_big, thr_big = run(big, big_rate, 100, seed + 2)
+        # the same ticks at lighter loads: where the tail comes from sharing the GPU
+        load_curve = {}
+        for frac, n_ticks in ((0.25, 100), (0.1, 60)):
+            lat_l, thr_l = run(big, frac * cap_big_hz, n_ticks, seed + 4)
+            load_curve[f"{int(frac * 100)}%"] = {"rate_hz": frac * cap_big_hz, "ticks": len(lat_l),
+                                                 "pairs_per_s": thr_l, **latency_summary(lat_l)}
 
         # phase 3: the pairs come from the device broad phase (boxes grown by one tick of
         # the fastest motion, 50 * dt), GJK + EPA on them, nothing on the host in between
@@ -530,6 +536,7 @@ def serving_report(device: int, seed: int = 77, slots: int = 4, max_in_flight: i
         "mixed": {"rate_hz": mix_rate, "ticks": len(lat_mix), "pairs_per_s": thr_mix, **latency_summary(lat_mix)},
         "ticks_200k": {"rate_hz": big_rate, "ticks": len(lat_big), "pairs_per_s": thr_big,
                        **latency_summary(lat_big)},
+        "ticks_200k_lighter_loads": load_curve,
         "broadphase_ticks": {"rate_hz": broad_rate, "ticks": len(lat_b), "cell": cell, "margin": margin,
                              "mean_pairs_per_tick": float(np.mean(found)),
                              "capacity_ticks_per_s": cap_broad_hz, **latency_summary(lat_b)},
