@@ -155,7 +155,7 @@ int default_choice(const std::vector<Launch>& vs, int b, bool epa) {
 
 ogx_status init_variant(Launch* k, bool epa, int sms) {
   const size_t staging = staging_bytes(variant_stages(k->K));
-  k->smem = epa ? ((size_t)(kBlock / k->L) * sizeof(EpaMemSmall) + 15) / 16 * 16 + staging : staging;
+  k->smem = epa ? (size_t)(kBlock / k->L) * epa_team_stride(k->L) + staging : staging;
   cudaError_t e;
   if (k->smem > 48 * 1024) {
     e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,

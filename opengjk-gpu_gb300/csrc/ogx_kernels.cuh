@@ -320,17 +320,25 @@ __device__ __forceinline__ bool epa_item(const WarpTeam<L>& t, const DevBatch& B
 // EPA over one bucket's contacts with the small working set (EpaMemSmall per team in
 // shared memory); contacts that need more than kEpaSmallIters expansions, or whose FP32
 // expansion met an inconsistent horizon, go to the spill list
+// Byte stride between the teams' working sets in shared memory: whole 128-byte lines
+// plus 4 L bytes, so that the teams of a warp start L banks apart and their lanes' 4-byte
+// and 1-byte accesses to the same field of their own working sets fall in different banks
+// (the unpadded 2288-byte sets started 28 banks apart, and lanes of neighbouring teams
+// met in the same banks: 466k conflicts in one 16-point EPA launch).
+OGX_HD constexpr size_t epa_team_stride(int L) {
+  return (sizeof(EpaMemSmall) + 127) / 128 * 128 + (L >= 4 ? (4 * (size_t)L) % 128 : 16);
+}
+
 // shared memory of k_epa: the teams' working sets, then the staging slots (D > 0)
 template <int L>
-OGX_HD constexpr size_t epa_mem_bytes() { return ((kStageStride / L) * sizeof(EpaMemSmall) + 15) / 16 * 16; }
+OGX_HD constexpr size_t epa_mem_bytes() { return (kStageStride / L) * epa_team_stride(L); }
 
 template <int L, int K, int OCC = 1, int D = 0, bool kPosed = false>
 __global__ void __launch_bounds__(kStageStride, OCC) k_epa(DevBatch B, int bucket) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  EpaMemSmall* mem = reinterpret_cast<EpaMemSmall*>(smem_raw);
   float4* slots = reinterpret_cast<float4*>(smem_raw + epa_mem_bytes<L>()) + threadIdx.x;
   const WarpTeam<L> t;
-  EpaMemSmall& M = mem[threadIdx.x / L];
+  EpaMemSmall& M = *reinterpret_cast<EpaMemSmall*>(smem_raw + (threadIdx.x / L) * epa_team_stride(L));
   const int team = (blockIdx.x * blockDim.x + threadIdx.x) / L;
   const int nteams = (gridDim.x * blockDim.x) / L;
   const int cnt = B.counts[kCntEpa + bucket];

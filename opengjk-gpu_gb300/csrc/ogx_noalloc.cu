@@ -101,7 +101,7 @@ ogx_status setup(int dev, Setup** out) {
     if (!g || !q) return ogx_fail(OGX_ERR_CUDA, "no kernel variant for bucket %d", b);
     s.gjk[b] = *g;
     s.epa[b] = *q;
-    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * sizeof(EpaMemSmall);
+    s.smem_epa[b] = (size_t)(kNoAllocBlock / q->L) * epa_team_stride(q->L);
     // launches here take no dynamic shared memory beyond the default 48 KB per block
     if (s.smem_epa[b] > 48 * 1024)
       return ogx_fail(OGX_ERR_CUDA, "EPA variant for bucket %d needs %zu B of shared memory (> 48 KB)", b,
