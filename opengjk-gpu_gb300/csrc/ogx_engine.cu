@@ -280,7 +280,7 @@ extern "C" ogx_status ogx_ctx_create(int device, const ogx_config* cfg, void* st
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
   cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
   if (major * 10 + minor != 103)
-    return ogx_fail(OGX_ERR_NO_DEVICE, "device %d is sm_%d%d; this build is sm_103a only", device,
+    return ogx_fail(OGX_ERR_NO_DEVICE, "device %d is sm_%d%d; the library is compiled for sm_103a only", device,
                     major, minor);
   ogx_config c = cfg ? *cfg : default_config();
   ogx_status s = check_config(c);
