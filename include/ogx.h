@@ -119,8 +119,11 @@ int64_t ogx_pool_num_points(const ogx_pool* pool);
 /* Load all points: xyz interleaved, bodies concatenated in index order (host memory,
  * pinned or pageable).  Asynchronous on the context's stream.  Page-locked sources are
  * read by the packing kernel directly over the host link (keep them unchanged until the
- * stream passes the call, as for any asynchronous copy); pageable ones are staged
- * through the context's pinned buffer. */
+ * stream passes the call, as for any asynchronous copy).  Pageable ones are read by the
+ * packing kernel directly too where the device reads pageable memory through the host's
+ * page tables (a Grace system), and the call returns once they are packed; elsewhere (or
+ * with OGX_UPLOAD_STAGED=1 in the environment) they are staged through the context's
+ * pinned buffer. */
 ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* pool, const float* coords);
 /* Same from device memory (xyz interleaved, concatenated): a packing kernel. */
 ogx_status ogx_pool_load_device(ogx_ctx* ctx, ogx_pool* pool, const float* d_coords);

@@ -309,25 +309,13 @@ void parallel_for(int n, int nt, F fn) {
   for (auto& t : th) t.join();
 }
 
-// Does the device read pageable host memory directly (through the host's page tables)?
-// Then host-buffer calls pack the caller's points on the device (k_pack_ptrs) instead of
-// gathering them on the host.  OGX_COMPAT_GATHER=1 in the environment forces the gather.
+// Host-buffer calls pack the caller's points on the device (k_pack_ptrs) where it reads
+// pageable host memory directly (ogx_pageable_reads); OGX_COMPAT_GATHER=1 in the
+// environment forces the host gather instead.
 bool pageable_reads(int dev) {
-  static std::atomic<int> known[kMaxDevices];  // 0 unknown, 1 no, 2 yes
-  if (dev < 0 || dev >= kMaxDevices) return false;
   const char* force = std::getenv("OGX_COMPAT_GATHER");
   if (force && force[0] == '1') return false;
-  int k = known[dev].load();
-  if (k == 0) {
-    int a = 0, t = 0;
-    const bool ok = cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
-                    cudaDeviceGetAttribute(&t, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
-                        cudaSuccess;
-    if (!ok) cudaGetLastError();
-    k = ok && a == 1 && t == 1 ? 2 : 1;
-    known[dev].store(k);
-  }
-  return k == 2;
+  return ogx_pageable_reads(dev);
 }
 
 bool is_pinned(const void* p) {

@@ -12,6 +12,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstdlib>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -477,6 +479,22 @@ extern "C" int ogx_ctx_work_counts(ogx_ctx* ctx, int32_t* counts, int cap) {
   return kCntSlots;
 }
 
+bool ogx_pageable_reads(int dev) {
+  static std::atomic<int> known[16];  // 0 unknown, 1 no, 2 yes
+  if (dev < 0 || dev >= 16) return false;
+  int k = known[dev].load();
+  if (k == 0) {
+    int a = 0, t = 0;
+    const bool ok = cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+                    cudaDeviceGetAttribute(&t, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) ==
+                        cudaSuccess;
+    if (!ok) cudaGetLastError();
+    k = ok && a == 1 && t == 1 ? 2 : 1;
+    known[dev].store(k);
+  }
+  return k == 2;
+}
+
 size_t ogx_scratch_bytes_per_pair() {
   return 2 * kBuckets * sizeof(int) + sizeof(PolishRec) + sizeof(RefineRec) + 2 * sizeof(int);
 }
@@ -645,6 +663,19 @@ extern "C" ogx_status ogx_pool_upload(ogx_ctx* ctx, ogx_pool* p, const float* co
     ogx_status s = pool_pack(ctx, p, static_cast<const float*>(attr.devicePointer));
     if (!s) ctx->last_launches = 1;
     return s;
+  }
+  const char* force = std::getenv("OGX_UPLOAD_STAGED");
+  if (!pinned && ogx_pageable_reads(ctx->device) && !(force && force[0] == '1')) {
+    // a device that reads pageable memory through the host's page tables packs straight
+    // from the caller's array too; the call then waits for the pack, since a pageable
+    // array may be changed or freed as soon as the call returns
+    ctx->last_launches = 0;
+    ogx_status s = pool_pack(ctx, p, coords);
+    if (s) return s;
+    ctx->last_launches = 1;
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return ogx_cuda_fail(e, "pool pack from host memory");
+    return OGX_OK;
   }
   ogx_status s = ctx->ensure_stage(pinned ? 0 : bytes, bytes);
   if (s) return s;

@@ -89,6 +89,10 @@ ogx_status ogx_cuda_fail(cudaError_t e, const char* what);
 ogx_status pool_pack(ogx_ctx* ctx, const ogx_pool* p, const float* d_aos);
 // bytes of a context's work lists per pair of capacity (ogx_ctx::ensure_scratch)
 size_t ogx_scratch_bytes_per_pair();
+// Does device dev read pageable host memory directly, through the host's page tables
+// (cudaDevAttrPageableMemoryAccess and ...UsesHostPageTables: the GPU of a Grace system
+// over NVLink-C2C)?  Queried once per device.
+bool ogx_pageable_reads(int dev);
 ogx_status ogx_run(ogx_ctx* ctx, const float* d_pool, const ogx::BodyRef* d_bodies, int nbodies,
                    int npairs, const gkCollisionPair* d_pairs, gkSimplex* d_smp, float* d_dist,
                    float* d_nrm, int32_t* d_status, int mode, const int2* d_warm = nullptr,

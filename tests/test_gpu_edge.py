@@ -176,6 +176,29 @@ def test_pinned_upload_reads_host_directly(engine):
     assert np.array_equal(ra["dist"], rb["dist"]) and np.array_equal(ra["normal"], rb["normal"])
 
 
+def test_pageable_upload_direct_or_staged_alike(engine, monkeypatch):
+    """A pageable source is packed straight from host memory where the device reads
+    pageable memory (a Grace system), else staged through pinned memory
+    (OGX_UPLOAD_STAGED=1): the same pool either way, and the call returns with the
+    source no longer needed (overwriting it afterwards changes nothing)."""
+    import torch
+    b = W.powerlaw(seed=45, n_pairs=3000)
+    ctx = engine.Context(0)
+    pairs = torch.from_numpy(np.ascontiguousarray(b.pairs)).cuda()
+    res = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("OGX_UPLOAD_STAGED", mode)
+        src = b.coords.copy()
+        pool = engine.Pool(ctx, b.counts)
+        pool.upload(src)
+        src[:] = np.nan  # the call returned: the pool no longer reads the source
+        res[mode] = engine.run(ctx, pool, pairs).to_host()
+        ctx.synchronize()
+    for k in ("dist", "normal", "status"):
+        assert np.array_equal(res["0"][k], res["1"][k])
+    assert np.isfinite(res["0"]["dist"]).all()
+
+
 @pytest.mark.parametrize("chunks", [1, 3, 8])
 def test_streamed_call_matches_batched(engine, chunks):
     """The host-to-host call with overlapped chunks gives the results of the device
