@@ -161,35 +161,6 @@ __global__ void k_desc_pack(DescSrc src, int nb, BodyRef* __restrict__ bodies, f
   }
 }
 
-// Pack from a table of coordinate pointers (one per body, xyz interleaved) that address
-// the caller's host arrays: on a device that reads pageable host memory through the host's
-// page tables (cudaDevAttrPageableMemoryAccess, the GPU of a Grace system over NVLink-C2C)
-// the kernel loads the points where the caller keeps them, so the host gathers nothing.
-// Bodies with a NaN or infinite coordinate are marked as k_pack does.
-__global__ void k_pack_ptrs(const float* const* __restrict__ src, int nb, BodyRef* __restrict__ bodies,
-                            float* __restrict__ pool) {
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (int b = warp; b < nb; b += nwarps) {
-    const BodyRef r = bodies[b];
-    const float* c = src[b];
-    const int n4 = round4(r.n);
-    float* dst = pool + 4 * (size_t)r.quad;
-    bool finite = true;
-    for (int i = lane; i < n4; i += 32) {
-      const int s = i < r.n ? i : 0;
-      const float x = c[3 * s], y = c[3 * s + 1], z = c[3 * s + 2];
-      finite = finite && is_finite(x) && is_finite(y) && is_finite(z);
-      dst[i] = x;
-      dst[n4 + i] = y;
-      dst[2 * n4 + i] = z;
-    }
-    finite = __all_sync(0xffffffffu, finite);
-    if (lane == 0 && !finite) bodies[b].n = -r.n;
-  }
-}
-
 // Bodies given in double (the *_f64 calls): every separated pair continues GJK in FP64 on
 // the caller's double points from the FP32 pass's final simplex -- exact supports and
 // exact Minkowski points, one thread per pair -- so its distance carries no rounding of
@@ -396,15 +367,28 @@ ogx_status pool_from_device_desc(Compat& c, DescSrc src, int nb) {
   return OGX_OK;
 }
 
-// Build the pool from descriptors in HOST memory with host coordinates.
-ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope* b, int nb) {
-  std::vector<int32_t> counts(nb);
-  std::vector<const float*> src(nb);
-  std::vector<int64_t> voff(nb);
-  std::vector<BodyRef> refs(nb);
-  // body table in two parallel passes over pieces of the descriptors: per piece the
-  // point and float4-block totals (and the first invalid descriptor), then, after a
-  // prefix over the pieces, every body's offsets
+// The pool's body table from host descriptors (pairs (a[i], b[i]) when b is given, else
+// the bodies of a), in two parallel passes over pieces of the descriptors: per piece the
+// point and float4-block totals (and the first invalid descriptor), then, after a prefix
+// over the pieces, every body's offsets.
+struct HostTables {
+  std::vector<int32_t> counts;
+  std::vector<const float*> src;
+  std::vector<int64_t> voff;
+  std::vector<BodyRef> refs;
+  int64_t pts = 0;
+  uint64_t quad = 0;
+};
+
+ogx_status host_tables(const gkPolytope* a, const gkPolytope* b, int nb, HostTables& T) {
+  T.counts.resize(nb);
+  T.src.resize(nb);
+  T.voff.resize(nb);
+  T.refs.resize(nb);
+  std::vector<int32_t>& counts = T.counts;
+  std::vector<const float*>& src = T.src;
+  std::vector<int64_t>& voff = T.voff;
+  std::vector<BodyRef>& refs = T.refs;
   const int nt = (int)std::min<int64_t>(16, std::max<int64_t>(1, nb >> 15));
   std::vector<int64_t> piece_pts(nt + 1, 0), piece_quad(nt + 1, 0);
   std::vector<int> bad(nt, -1);
@@ -433,9 +417,9 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
     piece_pts[k + 1] += piece_pts[k];
     piece_quad[k + 1] += piece_quad[k];
   }
-  const int64_t pts = piece_pts[nt];
-  const uint64_t quad = (uint64_t)piece_quad[nt];
-  if (quad >= (1ull << 32)) return ogx_fail(OGX_ERR_CAPACITY, "pool exceeds 2^32 float4 blocks");
+  T.pts = piece_pts[nt];
+  T.quad = (uint64_t)piece_quad[nt];
+  if (T.quad >= (1ull << 32)) return ogx_fail(OGX_ERR_CAPACITY, "pool exceeds 2^32 float4 blocks");
   parallel_for(nb, nt, [&](int lo, int hi, int k) {
     int64_t np = piece_pts[k], nq = piece_quad[k];
     for (int i = lo; i < hi; ++i) {
@@ -446,31 +430,53 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
       nq += 3 * (int64_t)((counts[i] + 3) / 4);
     }
   });
+  return OGX_OK;
+}
+
+// The body table, the coordinate pointers and the offsets up (a device that reads
+// pageable memory packs the points from the caller's arrays itself), the pool grown.
+ogx_status upload_tables(Compat& c, const HostTables& T, int nb) {
+  ogx_ctx* ctx = c.ctx;
+  cudaStream_t st = ctx->stream;
+  const size_t tb = nb * sizeof(BodyRef), pb = nb * sizeof(const float*), ob = nb * sizeof(int64_t);
+  ogx_status s = ctx->ensure_stage(tb + pb + ob, 0);
+  if (!s) s = grow(&c.d_bodies, &c.bodies_cap, (size_t)nb, "compat body table");
+  if (!s) s = grow(&c.d_src, &c.src_cap, (size_t)nb, "compat coordinate pointers");
+  if (!s) s = grow(&c.d_voff, &c.voff_cap, (size_t)nb, "compat offsets");
+  if (!s) s = grow(&c.d_points, &c.points_cap, 4 * (size_t)T.quad + 4, "compat pool");
+  if (s) return s;
+  cudaStreamSynchronize(st);  // staging buffers may still be read by a previous call
+  char* h = static_cast<char*>(ctx->h_stage);
+  parallel_copy(h, T.refs.data(), tb);
+  parallel_copy(h + tb, T.src.data(), pb);
+  parallel_copy(h + tb + pb, T.voff.data(), ob);
+  cudaError_t e = cudaMemcpyAsync(c.d_bodies, h, tb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_src, h + tb, pb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_voff, h + tb + pb, ob, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return ogx_cuda_fail(e, "body table upload");
+  return OGX_OK;
+}
+
+// Build the pool from descriptors in HOST memory with host coordinates.
+ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope* b, int nb) {
+  HostTables T;
+  ogx_status s0 = host_tables(a, b, nb, T);
+  if (s0) return s0;
+  const std::vector<int32_t>& counts = T.counts;
+  const std::vector<const float*>& src = T.src;
+  const std::vector<int64_t>& voff = T.voff;
+  const std::vector<BodyRef>& refs = T.refs;
+  const int64_t pts = T.pts;
+  const uint64_t quad = T.quad;
   ogx_ctx* ctx = c.ctx;
   cudaStream_t st = ctx->stream;
   const size_t bytes = (size_t)pts * 3 * sizeof(float);
   if (pageable_reads(ctx->device)) {
     // the body table and the coordinate pointers up, the points packed from where the
     // caller keeps them
-    const size_t tb = nb * sizeof(BodyRef), pb = nb * sizeof(const float*), ob = nb * sizeof(int64_t);
-    ogx_status s = ctx->ensure_stage(tb + pb + ob, 0);
-    if (!s) s = grow(&c.d_bodies, &c.bodies_cap, (size_t)nb, "compat body table");
-    if (!s) s = grow(&c.d_src, &c.src_cap, (size_t)nb, "compat coordinate pointers");
-    if (!s) s = grow(&c.d_voff, &c.voff_cap, (size_t)nb, "compat offsets");
-    if (!s) s = grow(&c.d_points, &c.points_cap, 4 * (size_t)quad + 4, "compat pool");
+    ogx_status s = upload_tables(c, T, nb);
     if (s) return s;
-    cudaStreamSynchronize(st);  // staging buffers may still be read by a previous call
-    char* h = static_cast<char*>(ctx->h_stage);
-    parallel_copy(h, refs.data(), tb);
-    parallel_copy(h + tb, src.data(), pb);
-    parallel_copy(h + tb + pb, voff.data(), ob);
-    cudaError_t e = cudaMemcpyAsync(c.d_bodies, h, tb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_src, h + tb, pb, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(c.d_voff, h + tb + pb, ob, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) {
-      k_pack_ptrs<<<8 * ctx->sm_count, 256, 0, st>>>(c.d_src, nb, c.d_bodies, c.d_points);
-      e = cudaGetLastError();
-    }
+    const cudaError_t e = launch_pack_ptrs(c.d_src, nb, c.d_bodies, c.d_points, 8 * ctx->sm_count, st);
     if (e != cudaSuccess) return ogx_cuda_fail(e, "polytope pack from host memory");
     return OGX_OK;
   }

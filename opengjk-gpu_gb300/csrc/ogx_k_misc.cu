@@ -284,6 +284,42 @@ __global__ void __launch_bounds__(128) k_polish(DevBatch B) {
 }
 
 
+// Pack from a table of coordinate pointers (one per body, xyz interleaved) that address
+// the caller's host arrays: on a device that reads pageable host memory through the host's
+// page tables (cudaDevAttrPageableMemoryAccess, the GPU of a Grace system over NVLink-C2C)
+// the kernel loads the points where the caller keeps them, so the host gathers nothing.
+// Bodies with a NaN or infinite coordinate are marked as k_pack does.
+__global__ void k_pack_ptrs(const float* const* __restrict__ src, int nb, BodyRef* __restrict__ bodies,
+                            float* __restrict__ pool) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int b = warp; b < nb; b += nwarps) {
+    const BodyRef r = bodies[b];
+    const float* c = src[b];
+    const int n4 = round4(r.n);
+    float* dst = pool + 4 * (size_t)r.quad;
+    bool finite = true;
+    for (int i = lane; i < n4; i += 32) {
+      const int s = i < r.n ? i : 0;
+      const float x = c[3 * s], y = c[3 * s + 1], z = c[3 * s + 2];
+      finite = finite && is_finite(x) && is_finite(y) && is_finite(z);
+      dst[i] = x;
+      dst[n4 + i] = y;
+      dst[2 * n4 + i] = z;
+    }
+    finite = __all_sync(0xffffffffu, finite);
+    if (lane == 0 && !finite) bodies[b].n = -r.n;
+  }
+}
+
+cudaError_t launch_pack_ptrs(const float* const* src, int nbodies, BodyRef* bodies, float* pool, int grid,
+                             cudaStream_t st) {
+  if (nbodies <= 0) return cudaSuccess;
+  k_pack_ptrs<<<grid, 256, 0, st>>>(src, nbodies, bodies, pool);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack(const float* aos, const int64_t* voff, BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st) {
   k_pack<<<grid, 256, 0, st>>>(aos, voff, bodies, nbodies, pool);

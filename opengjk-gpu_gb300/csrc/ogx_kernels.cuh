@@ -399,6 +399,11 @@ cudaError_t epa_spill_occupancy(int block, int* per_sm);
 cudaError_t refine_occupancy(int block, int* per_sm);
 cudaError_t launch_pack(const float* aos, const int64_t* voff, BodyRef* bodies, int nbodies,
                         float* pool, int grid, cudaStream_t st);
+// packs bodies whose points the device reads where the caller keeps them (src[b]: xyz of
+// body b, host memory of a device that reads pageable memory); bodies[] already holds
+// each body's count and pool offset
+cudaError_t launch_pack_ptrs(const float* const* src, int nbodies, BodyRef* bodies, float* pool, int grid,
+                             cudaStream_t st);
 cudaError_t launch_bin(const DevBatch& B, int grid, cudaStream_t st);
 cudaError_t launch_polish(const DevBatch& B, int grid, cudaStream_t st);
 cudaError_t polish_occupancy(int block, int* per_sm);
