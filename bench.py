@@ -281,6 +281,65 @@ def cpu_baseline(batch, seconds: float = 12.0, mode="gjk_epa"):
             "cpu_model": cpu_model(), "cores_1": cpu_single_thread(batch)}
 
 
+def fp64_plain_report(calls: int = 20) -> dict:
+    """The FP64 plain-GJK configuration (1,000 pairs of 32-point bodies on spheres, radius
+    U[0.5, 2], centres U[-5, 5]^3, double coordinates) through the FP64 drop-in
+    (`ogx_compute_minimum_distance_f64`: double descriptors in, 184-byte simplices and
+    double distances out, host arrays), median host time of `calls` calls; beside it the
+    reference's FP64 CPU GJK (the oracle, which is pinned to it bit for bit) on the same
+    inputs, one thread and all host threads."""
+    import ctypes
+    from ogx import _lib, workloads as W
+    from oracle import orc
+    b = W.plain(seed=1000, n_pairs=1000, dtype=np.float64)
+    c64 = np.ascontiguousarray(b.coords)
+    poly = np.dtype([("numpoints", "<i4"), ("s", "<f8", (3,)), ("s_idx", "<i4"), ("coord", "<u8")], align=True)
+    smp_t = np.dtype([("nvrtx", "<i4"), ("vrtx", "<f8", (4, 3)), ("vrtx_idx", "<i4", (4, 2)),
+                      ("witnesses", "<f8", (2, 3))], align=True)
+
+    def desc(idx):
+        d = np.zeros(len(idx), poly)
+        d["numpoints"] = b.counts[idx]
+        d["coord"] = c64.ctypes.data + 24 * b.offsets[idx].astype(np.uint64)
+        return d
+    d1, d2 = desc(b.pairs[:, 0]), desc(b.pairs[:, 1])
+    n = b.n_pairs
+    smp, dist = np.zeros(n, smp_t), np.zeros(n)
+    L = _lib.load()
+    fn = L.ogx_compute_minimum_distance_f64
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
+    args = (n, d1.ctypes.data, d2.ctypes.data, smp.ctypes.data, dist.ctypes.data)
+    for _ in range(3):
+        _lib.check(fn(*args))
+    ts = []
+    for _ in range(calls):
+        t = time.perf_counter()
+        _lib.check(fn(*args))
+        ts.append(time.perf_counter() - t)
+    ms = float(np.median(ts)) * 1e3
+    o = orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK, precision="f64")
+    sep = o["dist"] > 1e-5 * np.maximum(1.0, np.abs(c64).max())
+    rel = float(np.max(np.abs(dist[sep] - o["dist"][sep]) / o["dist"][sep])) if sep.any() else 0.0
+    cpu = {}
+    for threads in (1, os.cpu_count() or 1):
+        reps, t = 0, time.perf_counter()
+        while True:
+            orc.run(b.coords, b.offsets, b.counts, b.pairs, mode=orc.MODE_GJK, precision="f64", threads=threads)
+            reps += 1
+            dt = time.perf_counter() - t
+            if dt >= 0.5 or reps >= 200:
+                break
+        cpu[f"threads_{threads}"] = reps * n / dt
+    return {"workload": "plain GJK, FP64, 1,000 pairs, 32 points per body on spheres (radius U[0.5, 2], "
+                        "centres U[-5, 5]^3), seed 1000",
+            "value": n / (ms / 1e3), "unit": "pairs/s", "ms_per_call": ms,
+            "path": "ogx_compute_minimum_distance_f64, host arrays in and out, host clock, median of "
+                    f"{calls} calls",
+            "max_rel_err_vs_fp64_oracle": rel,
+            "cpu_fp64_pairs_per_s": cpu, "cpu_kind": "port (the reference's CPU GJK restated, pinned to it)"}
+
+
 def plain_form_baseline(batch, device: int, steps: int = 3) -> dict:
     """The reference's own GPU kernels (GJK/gpu/openGJK.cu, FP32 as shipped, compiled for
     sm_103a) on the same workload with the points resident: its fused indexed call's
@@ -820,6 +879,8 @@ def run_ours(args):
         line["parity"]["source"] = "profiles/parity_powerlaw_1M.json (tests/test_gpu_fullsize.py, same batch)"
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(batch)
+        if world == 1:
+            line["fp64_plain_1k"] = fp64_plain_report()
     if not args.no_plain and world == 1:
         line["plain_form"] = plain_form_baseline(batch, local)
         if "value" in line["plain_form"]:
