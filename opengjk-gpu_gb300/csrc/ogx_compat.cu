@@ -23,6 +23,9 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <condition_variable>
+#include <deque>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -253,6 +256,77 @@ ogx_status grow(T** p, size_t* cap, size_t need, const char* what) {
   return OGX_OK;
 }
 
+// Host worker threads for the calls' parallel host loops, started on first use and kept
+// for the process (a call used to start up to 16 threads for each of its loops, ~100
+// thread starts a call).  run(n, fn) runs fn(k) for k = 1..n-1 on the workers and fn(0)
+// on the caller, and returns when all have run; calls from several host threads share
+// the workers (their pieces queue in order).
+class HostWorkers {
+ public:
+  static HostWorkers& get() {
+    static HostWorkers w;
+    return w;
+  }
+  int size() const { return (int)threads_.size(); }
+  void run(int n, const std::function<void(int)>& fn) {
+    if (n <= 1 || threads_.empty()) {
+      for (int k = 0; k < std::max(n, 1); ++k) fn(k);
+      return;
+    }
+    Group g{&fn, 0};
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      for (int k = 1; k < n; ++k) queue_.push_back(Task{&g, k});
+    }
+    cv_.notify_all();
+    fn(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return g.done == n - 1; });
+  }
+  ~HostWorkers() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : threads_) t.join();
+  }
+
+ private:
+  struct Group {
+    const std::function<void(int)>* fn;
+    int done;
+  };
+  struct Task {
+    Group* g;
+    int k;
+  };
+  HostWorkers() {
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int n = std::max(0, std::min(15, hw - 1));
+    for (int i = 0; i < n; ++i) threads_.emplace_back([this] { loop(); });
+  }
+  void loop() {
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      cv_.wait(lk, [&] { return stop_ || !queue_.empty(); });
+      if (queue_.empty()) return;  // stopping
+      const Task t = queue_.front();
+      queue_.pop_front();
+      lk.unlock();
+      (*t.g->fn)(t.k);
+      lk.lock();
+      ++t.g->done;
+      done_cv_.notify_all();
+    }
+  }
+  std::vector<std::thread> threads_;
+  std::deque<Task> queue_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  bool stop_ = false;
+};
+
 // Host copy of `bytes` bytes on up to 16 threads (one for small copies).
 void parallel_copy(void* dst, const void* src, size_t bytes) {
   const int nt = (int)std::min<size_t>(16, std::max<size_t>(1, bytes >> 22));
@@ -260,24 +334,17 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
     memcpy(dst, src, bytes);
     return;
   }
-  std::vector<std::thread> th;
-  for (int k = 0; k < nt; ++k)
-    th.emplace_back([=] {
-      const size_t a = bytes * k / nt, b = bytes * (k + 1) / nt;
-      memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, b - a);
-    });
-  for (auto& t : th) t.join();
+  HostWorkers::get().run(nt, [=](int k) {
+    const size_t a = bytes * k / nt, b = bytes * (k + 1) / nt;
+    memcpy(static_cast<char*>(dst) + a, static_cast<const char*>(src) + a, b - a);
+  });
 }
 
-// fn(lo, hi, k) over [0, n) in nt contiguous pieces, piece k on its own thread (the
-// caller's thread takes piece 0)
+// fn(lo, hi, k) over [0, n) in nt contiguous pieces, piece k on a worker (the caller's
+// thread takes piece 0)
 template <class F>
 void parallel_for(int n, int nt, F fn) {
-  std::vector<std::thread> th;
-  for (int k = 1; k < nt; ++k)
-    th.emplace_back([&, k] { fn((int)((int64_t)n * k / nt), (int)((int64_t)n * (k + 1) / nt), k); });
-  fn(0, (int)((int64_t)n / nt), 0);
-  for (auto& t : th) t.join();
+  HostWorkers::get().run(nt, [&](int k) { fn((int)((int64_t)n * k / nt), (int)((int64_t)n * (k + 1) / nt), k); });
 }
 
 // Host-buffer calls pack the caller's points on the device (k_pack_ptrs) where it reads
@@ -490,32 +557,29 @@ ogx_status pool_from_host_desc(Compat& c, const gkPolytope* a, const gkPolytope*
   // Gather the coordinates into the pinned staging in pieces of bodies, on up to 16
   // threads, and upload each piece as soon as it is gathered: the copy engine moves piece
   // k while the threads gather piece k + 1.
-  const int gt = (int)std::min<int64_t>(16, std::max<int64_t>(1, pts >> 18));
+  // (no more shares than workers + this thread: share 0 waits for the others' pieces)
+  const int gt = (int)std::min<int64_t>(std::min(16, HostWorkers::get().size() + 1), std::max<int64_t>(1, pts >> 18));
   const int pieces = bytes >= ((size_t)64 << 20) ? 8 : 1;
   std::vector<std::atomic<int>> gathered(pieces);
   for (auto& g : gathered) g.store(0);
   auto piece_begin = [&](int pc) { return (int)((int64_t)nb * pc / pieces); };
-  std::vector<std::thread> th;
-  for (int k = 1; k < gt; ++k)
-    th.emplace_back([&, k] {
-      for (int pc = 0; pc < pieces; ++pc) {
-        const int i0 = piece_begin(pc), i1 = piece_begin(pc + 1);
-        for (int i = (int)(i0 + (int64_t)(i1 - i0) * k / gt); i < (int)(i0 + (int64_t)(i1 - i0) * (k + 1) / gt); ++i)
-          memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
-        gathered[pc].fetch_add(1);
-      }
-    });
+  // shares 1..gt-1 of every piece on the workers, share 0 and the uploads on this thread
   cudaError_t e = cudaSuccess;
-  for (int pc = 0; pc < pieces; ++pc) {
-    const int i0 = piece_begin(pc), i1 = piece_begin(pc + 1);
-    for (int i = i0; i < (int)(i0 + (int64_t)(i1 - i0) / gt); ++i)  // this thread's share
-      memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
-    while (gathered[pc].load() < gt - 1) std::this_thread::yield();
-    const size_t b0 = (size_t)voff[i0] * 12, b1 = i1 < nb ? (size_t)voff[i1] * 12 : bytes;
-    if (e == cudaSuccess && b1 > b0)
-      e = cudaMemcpyAsync(static_cast<char*>(ctx->d_stage) + b0, h + b0, b1 - b0, cudaMemcpyHostToDevice, st);
-  }
-  for (auto& t : th) t.join();
+  HostWorkers::get().run(gt, [&](int k) {
+    for (int pc = 0; pc < pieces; ++pc) {
+      const int i0 = piece_begin(pc), i1 = piece_begin(pc + 1);
+      for (int i = (int)(i0 + (int64_t)(i1 - i0) * k / gt); i < (int)(i0 + (int64_t)(i1 - i0) * (k + 1) / gt); ++i)
+        memcpy(h + voff[i] * 12, src[i], (size_t)counts[i] * 12);
+      if (k > 0) {
+        gathered[pc].fetch_add(1);
+        continue;
+      }
+      while (gathered[pc].load() < gt - 1) std::this_thread::yield();
+      const size_t b0 = (size_t)voff[i0] * 12, b1 = i1 < nb ? (size_t)voff[i1] * 12 : bytes;
+      if (e == cudaSuccess && b1 > b0)
+        e = cudaMemcpyAsync(static_cast<char*>(ctx->d_stage) + b0, h + b0, b1 - b0, cudaMemcpyHostToDevice, st);
+    }
+  });
   memcpy(h + bytes, refs.data(), nb * sizeof(BodyRef));
   memcpy(h + bytes + nb * sizeof(BodyRef), voff.data(), nb * sizeof(int64_t));
   if (e == cudaSuccess)
